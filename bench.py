@@ -1,0 +1,461 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 dynamical-core hot path.
+
+Metric: T42L20 member-steps/s of the batched ensemble (512 members, FP32
+state, seeded heatings, plain damping) through the fused stepper; a "step"
+is one semi-implicit leapfrog step of every member.  The synthetic workload
+is defined in lbm_isca_gb300/configs.py (no dataset is involved).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  Under torchrun each rank integrates its own
+512 members (weak scaling, no collective in the step); the timed region is
+bracketed by a barrier and device synchronisation and the max over ranks is
+reported.  `--impl reference` times the CPU reference algorithm (the numpy
+oracle restatement, oracle/lbm_oracle.py) on this host's cores.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import signal
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "T42L20 member-steps/s, batched mixed-prec vs plain FP64 at <=1e-5 rel L2 err"
+UNIT = "member-steps/s"
+GRID = (128, 64, 42)
+K_LEV = 20
+SEED = 1
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=720)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--members", type=int, default=512)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the accuracy / plain-FP64 / CPU side measurements")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the oracle (reference algorithm) on the host cores
+# ---------------------------------------------------------------------------
+def _oracle_worker(args):
+    """One single-member T42L20 oracle run; returns (steps, seconds)."""
+    member, warm, budget_s, max_steps = args
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    from oracle import lbm_oracle as orc
+    from lbm_isca_gb300 import configs
+    nlon, nlat, nmax = GRID
+    sigm = configs.equal_sigma_half_levels(K_LEV)
+    heats, _ = configs.ensemble_heating(nlon, nlat, sigm, member + 1, seed=SEED)
+    tr = orc.SphericalTransform(nlon, nlat, nmax)
+    lv = orc.SigmaLevels(sigm)
+    bs = configs.solid_body_basic_state(nlon, nlat, sigm)
+    m = orc.OracleModel(tr, lv, bs, orc.RunConfig(**configs.plain_damping(K_LEV)))
+    frc = heats[member]
+    for _ in range(warm):
+        m.step(frc_t=frc)
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_steps and (time.perf_counter() - t0) < budget_s:
+        m.step(frc_t=frc)
+        n += 1
+    return n, time.perf_counter() - t0
+
+
+def cpu_oracle_throughput(nproc, warm, budget_s, max_steps=10 ** 9):
+    """member-steps/s of `nproc` concurrent single-thread oracle runs."""
+    ctx = mp.get_context("spawn")
+    env_keys = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+    saved = {k: os.environ.get(k) for k in env_keys}
+    for k in env_keys:
+        os.environ[k] = "1"
+    try:
+        with ctx.Pool(nproc) as pool:
+            res = pool.map(_oracle_worker, [(e, warm, budget_s, max_steps)
+                                            for e in range(nproc)])
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    rate = sum(n / s for n, s in res)
+    return rate, res
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def reference_arm(args):
+    """`--impl reference`: the reference algorithm on the host cores."""
+    cores = min(host_cores(), 64)
+    # each worker: W warm-up steps, then up to K steps (bounded in time)
+    budget = max(5.0, min(120.0, args.cpu_seconds * 4))
+    rate, res = cpu_oracle_throughput(cores, max(1, min(args.warmup, 3)), budget,
+                                      max_steps=args.steps)
+    steps = int(min(n for n, _ in res))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * cores / rate if rate else None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "T42L20 solid-body basic state, seeded elliptic heatings "
+                               "(seed 1), plain damping; one member per host process",
+                   "members": cores, "grid": "T42 128x64", "levels": 20},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cores} concurrent single-thread numpy oracle runs, "
+                                   f"{steps}+ steps each"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+                start_new_session=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc is not None:
+            try:
+                os.killpg(self.proc.pid, signal.SIGTERM)
+            except Exception:
+                pass
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.out = ""
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r)
+                          if v.lower() == "active"})
+        return {"sm_mhz": float(np.median([r[0] for r in rows])),
+                "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons,
+                "samples": len(rows)}
+
+
+def build_model(E, precision, torch, days=1.0, seed=SEED, device="cuda"):
+    from lbm_isca_gb300 import configs
+    from lbm_isca_gb300.ensemble import make_ensemble_model
+    from lbm_isca_gb300.model import Config
+    nlon, nlat, nmax = GRID
+    sigm = configs.equal_sigma_half_levels(K_LEV)
+    bs = configs.solid_body_basic_state(nlon, nlat, sigm)
+    cfg = Config(ndays=days, precision=precision, **configs.plain_damping(K_LEV))
+    model, spb, vg = make_ensemble_model(bs, E, cfg, device=device, nlon=nlon, nlat=nlat,
+                                         nmax=nmax, sigm=sigm)
+    heats, _ = configs.ensemble_heating(nlon, nlat, sigm, E, seed=seed)
+    return model, heats
+
+
+def algorithmic_bytes(E, p):
+    """HBM bytes each stepper kernel must move per launch (p = bytes/real)."""
+    nlon, nlat, nmax = GRID
+    M, J, I, K = nmax + 1, nlat, nlon, K_LEV
+    NS = M * (M + 1) // 2
+    c = 2 * p
+    shared_grid = p * (10 * J * K * I + J * (K + 1) * I + 5 * J * I)
+    sf = c * M * J * (6 * K + 5)
+    af = c * M * J * (7 * K + 2)
+    st3 = c * 4 * NS * K
+    return {
+        "grid": E * (sf + af + 4 * p * J * I) + shared_grid,
+        "anal": E * (af + c * (4 * NS * K + 2 * NS)),
+        "implicit": E * (3 * st3 + c * 2 * NS + 2 * st3 + c * 4 * NS),
+        "synth": E * (st3 + c * 4 * NS + sf),
+    }
+
+
+def read_traffic(kernel, E):
+    """dram bytes per launch from the committed ncu summary, scaled to E."""
+    path = os.path.join(ROOT, "profiles", "ncu_summary.md")
+    if not os.path.exists(path):
+        return None
+    key = f"traffic[{kernel}]"
+    for line in open(path):
+        if line.strip().startswith(key):
+            try:
+                rhs = line.split("=", 1)[1].split()
+                val, members = float(rhs[0]), float(rhs[rhs.index("members") - 1])
+                return val * E / members
+            except Exception:
+                return None
+    return None
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            reference_arm(args)
+        return
+
+    # CPU baseline first, before any CUDA call (spawned pool, rank 0, N = 1)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_extras:
+        cores = min(host_cores(), 64)
+        rate, res = cpu_oracle_throughput(cores, 1, args.cpu_seconds)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{cores} concurrent single-thread numpy oracle runs of one T42L20 "
+                         f"member each, {min(n for n, _ in res)}+ steps in "
+                         f"{args.cpu_seconds:.0f} s"}
+
+    import torch
+    import torch.distributed as dist
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from lbm_isca_gb300 import _lib
+    from lbm_isca_gb300._lib import StepCtl, check, lib
+    from lbm_isca_gb300.backend import stream_handle
+    import ctypes as C
+
+    E = args.members
+    model, heats = build_model(E, args.precision, torch, seed=SEED + rank)
+    from lbm_isca_gb300.ensemble import EnsembleForcing
+    stp = model.stepper()
+    delt = model.cfg.delt
+    sched = model._schedule(args.warmup + args.steps + 1)
+    stp.set_timesteps(sorted({dt for dt, _ in sched}))
+    frc = model._spec_forcing(torch.as_tensor(heats, device="cuda"), True)
+    stp.set_forcing(frc_t=frc, per_member=True)
+    model._load_stepper(stp)
+    # forward start + warm-up (the first advancing step carries ps_mode 1)
+    n_start = model.cfg.inistp + 1
+    stp.run(sched[:n_start], use_graph=False)
+    stp.run(sched[n_start:n_start + args.warmup], use_graph=True)
+    torch.cuda.synchronize()
+
+    # ---- timed region: K steps, per-kernel CUDA events on the stepper stream ----
+    planned, _ = stp.plan([(delt, False)] * args.steps)
+    ctl = stp._ctl(planned[:1])
+    d = stp.desc()
+    L = lib()
+    sh = stream_handle(stp.stream)
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(5)]
+           for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_wall = time.perf_counter()
+        with torch.cuda.stream(stp.stream):
+            for s in range(args.steps):
+                ev = evs[s]
+                ev[0].record(stp.stream)
+                for kern in range(4):
+                    check(L.lbm_stepper_launch(C.byref(d), ctl, kern, sh), "launch")
+                    ev[kern + 1].record(stp.stream)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    stp.pending_ps_mode = 2
+    if world > 1:
+        dist.barrier()
+    total_ms = evs[0][0].elapsed_time(evs[-1][4])
+    kern_ms = np.zeros(4)
+    for ev in evs:
+        for kern in range(4):
+            kern_ms[kern] += ev[kern].elapsed_time(ev[kern + 1])
+    kern_ms /= args.steps
+    t_max = total_ms
+    if world > 1:
+        tt = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = world * E * args.steps / (t_max / 1000.0)
+    finite = stp.check_finite()
+
+    # ---- graph replay of the same steps (informational) ----
+    torch.cuda.synchronize()
+    g0 = torch.cuda.Event(enable_timing=True)
+    g1 = torch.cuda.Event(enable_timing=True)
+    g0.record(stp.stream)
+    stp.run([(delt, False)] * args.steps, use_graph=True, graph_chunk=72)
+    g1.record(stp.stream)
+    torch.cuda.synchronize()
+    graph_ms = g0.elapsed_time(g1) / args.steps
+
+    # ---- end to end through the public API, host buffers ----
+    e2e = None
+    if rank == 0:
+        days = args.steps / model.cfg.steps_per_day
+        m2, _ = build_model(E, args.precision, torch, days=days, seed=SEED + rank)
+        m2.stepper()
+        host_heat = torch.from_numpy(heats.astype(np.float64)).pin_memory()
+        warm = torch.empty(1, device="cuda")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dev_heat = host_heat.to("cuda", non_blocking=True)
+        m2.run(mjo_forcing=EnsembleForcing(dev_heat, device="cuda"), verbose=False)
+        out = {k: getattr(m2.ga, k).to("cpu") for k in ("u", "v", "t", "q", "ps")}
+        torch.cuda.synchronize()
+        t_e2e = time.perf_counter() - t0
+        nb_in = host_heat.numel() * host_heat.element_size()
+        nb_out = sum(x.numel() * x.element_size() for x in out.values())
+        e2e = {"value": E * args.steps / t_e2e, "unit": UNIT,
+               "h2d_bytes_per_step": nb_in / args.steps,
+               "d2h_bytes_per_step": nb_out / args.steps,
+               "seconds": t_e2e,
+               "note": "LBM.run of the ensemble from host heatings (H2D inside), "
+                       f"{args.steps} advancing + {m2.cfg.inistp} start-up steps, final "
+                       "grid state copied to host (D2H inside)"}
+        del m2
+
+    # ---- extras: accuracy vs FP64 and the plain single-member FP64 rate ----
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        extras = side_measurements(args, torch)
+
+    if rank == 0:
+        p = 4 if args.precision == "fp32" else 8
+        ab = algorithmic_bytes(E, p)
+        names = ["grid", "anal", "implicit", "synth"]
+        top = int(np.argmax(kern_ms))
+        peaks = {}
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except Exception:
+            pass
+        peak = float(peaks.get("hbm_gbs", 6800.0))
+        achieved = ab[names[top]] / (kern_ms[top] / 1000.0) / 1e9
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if args.precision == "fp32" else "f64", "data": "synthetic",
+            "config": {"workload": f"{E}-member T42L20 ensemble (solid-body basic state, "
+                                   f"seeded elliptic heatings seed {SEED}+rank, plain "
+                                   "damping), FP32 state, fused stepper",
+                       "members_per_gpu": E, "grid": "T42 128x64 Gaussian",
+                       "levels": "L20 equal sigma", "dt_s": delt,
+                       "l2": "inputs larger than L2 (per-step working set "
+                             f"{sum(ab.values()) / 1e9:.2f} GB)",
+                       "parallelism": f"members sharded, {world} independent rank(s)"},
+            "clocks": clk.summary(),
+            "e2e": e2e,
+            "gpu_launches": 4 * args.steps,
+            "roofline": {"bound": "hbm", "kernel": names[top], "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": read_traffic(names[top], E),
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+            "kernel_ms": dict(zip(names, [float(x) for x in kern_ms])),
+            "kernel_share": dict(zip(names, [float(x / kern_ms.sum()) for x in kern_ms])),
+            "algorithmic_gbs": {n: ab[n] / (kern_ms[i] / 1000.0) / 1e9
+                                for i, n in enumerate(names)},
+            "graph_ms_per_step": graph_ms,
+            "wall_s_timed": t_wall,
+            "finite": finite,
+            "cpu_baseline": cpu,
+        }
+        line.update(extras)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def side_measurements(args, torch):
+    """FP32-vs-FP64 relative L2 after 10 days (8 members) and the plain
+    single-member FP64 GPU rate that the batched rate is compared with."""
+    out = {}
+    nday = 10
+    E = 8
+    res = {}
+    for prec in ("fp64", "fp32"):
+        m, heats = build_model(E, prec, torch, days=nday)
+        from lbm_isca_gb300.ensemble import EnsembleForcing
+        m.run(mjo_forcing=EnsembleForcing(heats, device="cuda"), verbose=False)
+        a, _ = m.stepper().spectral_state()
+        res[prec] = {k: v.cpu().numpy() for k, v in a.items()}
+    rel = {}
+    for k in ("vor", "div", "t", "pi"):
+        r, f = res["fp64"][k], res["fp32"][k]
+        rel[k] = float(np.linalg.norm(f - r) / np.linalg.norm(r))
+    rel["q_absmax"] = float(np.abs(res["fp32"]["q"]).max())
+    out["accuracy_fp32_vs_fp64_day10"] = rel
+    # plain single-member FP64 GPU path
+    m1, heats = build_model(1, "fp64", torch, days=1.0)
+    stp = m1.stepper()
+    sched = m1._schedule(200)
+    stp.set_timesteps(sorted({dt for dt, _ in sched}))
+    stp.set_forcing(frc_t=m1._spec_forcing(torch.as_tensor(heats, device="cuda"), True),
+                    per_member=True)
+    m1._load_stepper(stp)
+    stp.run(sched[:3], use_graph=False)
+    stp.run([(m1.cfg.delt, False)] * 20, use_graph=True)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    n = 200
+    e0.record(stp.stream)
+    stp.run([(m1.cfg.delt, False)] * n, use_graph=True)
+    e1.record(stp.stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / n
+    out["plain_fp64_single_member"] = {"ms_per_step": ms, "member_steps_per_s": 1000.0 / ms}
+    return out
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,264 @@
+/*
+ * lbm_gb300 -- C ABI of the GB300 (sm_103a) dynamical-core hot path for the
+ * PyLBM-Isca linear baroclinic model.
+ *
+ * Every entry point takes device pointers, plain sizes and a CUDA stream
+ * (cudaStream_t passed as void*), launches asynchronously on that stream and
+ * returns an int status (LBM_OK = 0).  No C++ exception crosses the ABI and
+ * the library allocates no device memory: every buffer is owned by the
+ * caller.  Arrays are C-contiguous; "complex" means interleaved (re, im)
+ * pairs of the working precision; `prec` selects LBM_F64 (double) or
+ * LBM_F32 (float) for every array marked (R).
+ *
+ * Index conventions follow the reference (pylbm_isca): latitudes north to
+ * south, longitudes from 0 east, levels bottom-up (k = 0 is the lowest
+ * layer), spectral coefficients indexed [m][n] with n >= m.
+ *   M = nmax + 1; NS = M (M + 1) / 2 ("packed": rows (m, n), n = m..nmax,
+ *   m-major, row index = m M - m (m - 1) / 2 + n - m).
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------- */
+#define LBM_OK 0
+#define LBM_ERR_ARG 1          /* bad size, null pointer or unsupported grid   */
+#define LBM_ERR_LAUNCH 2       /* CUDA launch or runtime failure               */
+#define LBM_ERR_SINGULAR 3     /* zero pivot in a factorisation                */
+#define LBM_ERR_NONFINITE 4    /* non-finite prognostic value detected         */
+
+/* ---- precisions ------------------------------------------------------------- */
+#define LBM_F64 0
+#define LBM_F32 1
+
+/* Library version string. */
+const char* lbm_version(void);
+
+/* ============================================================================
+ * Setup (always FP64)
+ * ==========================================================================*/
+
+/* Gauss-Legendre nodes and weights, north first, weights summing to 1.
+ * Replaces numpy leggauss + sort + /2 at spectral.py:58-61.
+ * mu[nlat], gw[nlat]. */
+int lbm_gauss_legendre(int nlat, double* mu, double* gw, void* stream);
+
+/* Fully normalised associated Legendre functions P[m][n][j] (no
+ * Condon-Shortley phase, (1/2) int P^2 = 1) and H = (1 - mu^2) dP/dmu for
+ * 0 <= m, n <= nmax (zero for n < m); replaces Spectral._build_legendre,
+ * spectral.py:93-154.  pnm, hnm: [M][M][nlat]. */
+int lbm_legendre_tables(int nmax, int nlat, const double* mu, double* pnm,
+                        double* hnm, void* stream);
+
+/* exp(-2 pi i p / nlon) for p < nlon, complex FP64 [nlon]; twiddles of the
+ * longitude FFT (the role numpy's rfft plays at spectral.py:159-172). */
+int lbm_fft_twiddles(int nlon, double* tw, void* stream);
+
+/* Per-n gravity-wave matrices of the semi-implicit scheme,
+ *   M(n) = diag(fd ft) - dt^2 lap(n) (whmtx + gcmtx ft),
+ *   ft = 1 + 2 dt ktt[n], fd = 1 + 2 dt kd[n]
+ * (SemiImplicit.prepare, integrator.py:149-158).
+ * lap[M], ktt/kd[M][K], whmtx/gcmtx[K][K] -> mats[M][K][K]. */
+int lbm_gravity_wave_matrices(int nmax, int kmax, double dt, const double* lap,
+                              const double* ktt, const double* kd,
+                              const double* whmtx, const double* gcmtx,
+                              double* mats, void* stream);
+
+/* Batched inverse by Gauss-Jordan elimination with partial pivoting, FP64
+ * (xp.linalg.inv at integrator.py:161 and numpy inv at integrator.py:226).
+ * a, ainv: [batch][n][n]; info[batch] = 0, or 1 + the column of a zero pivot
+ * (then LBM_ERR_SINGULAR is reported by lbm_check_info). n <= 64. */
+int lbm_batched_inverse(int batch, int n, const double* a, double* ainv,
+                        int* info, void* stream);
+
+/* ============================================================================
+ * Spectral transforms on the reference layouts  (spectral.py:159-276)
+ *   grid    (R)       [batch][nlat][nlon][ncol]
+ *   Fourier (R, cplx) [batch][M][nlat][ncol]
+ *   spectral(R, cplx) [batch][M][M][ncol]   rectangle, zero for n < m
+ * ==========================================================================*/
+
+/* four = jscale[j] / nlon * rfft(grid) along longitude, m < M
+ * (Spectral._fft_fwd, spectral.py:159-164).  jscale (R)[nlat] or NULL.
+ * tw: twiddles (R, complex)[nlon] from lbm_fft_twiddles. nlon in {64,128,256}. */
+int lbm_fourier_forward(int prec, int batch, int nlat, int nlon, int ncol,
+                        int nmax, const void* grid, const void* jscale,
+                        const void* tw, void* four, void* stream);
+
+/* grid = jscale[j] * irfft(nlon * four) (Spectral._fft_inv,
+ * spectral.py:166-172; imaginary part of m = 0 dropped). */
+int lbm_fourier_inverse(int prec, int batch, int nlat, int nlon, int ncol,
+                        int nmax, const void* four, const void* jscale,
+                        const void* tw, void* grid, void* stream);
+
+/* Legendre analysis (the matmuls of spectral.py:190, 242-243):
+ *   spec[b][m][n][c] (+)= nfac[n] * ( ca * sum_j ta[m][n][j] fa[b][m][j][c]
+ *                                    + cb * sum_j tb[m][n][j] fb[b][m][j][c] )
+ * where ca = i m if ima else 1 (likewise cb with imb) times sign sb for the
+ * second term.  fb/tb may be NULL; nfac (R)[M] may be NULL; tables (R)
+ * [M][M][nlat]; accumulate = 0 overwrites (and zeroes n < m). */
+int lbm_legendre_analysis(int prec, int batch, int nmax, int nlat, int ncol,
+                          const void* fa, const void* ta, int ima,
+                          const void* fb, const void* tb, int imb, double sb,
+                          const void* nfac, int accumulate, void* spec,
+                          void* stream);
+
+/* Legendre synthesis (spectral.py:196, 220-221, 271-272):
+ *   four[b][m][j][c] = sum_n ta[m][n][j] ca na[n] sa[b][m][n][c]
+ *                    + sb * sum_n tb[m][n][j] cb nb[n] sb_[b][m][n][c]
+ * ca/cb = i m when ima/imb; na/nb (R)[M] may be NULL (= 1). */
+int lbm_legendre_synthesis(int prec, int batch, int nmax, int nlat, int ncol,
+                           const void* sa, const void* ta, int ima,
+                           const void* na, const void* sb_, const void* tb,
+                           int imb, const void* nb, double sb, void* four,
+                           void* stream);
+
+/* ============================================================================
+ * Linearised tendency, grid-point part  (Dynamics.tendencies,
+ * dynamics.py:176-267) on the reference grid layout, one launch for all the
+ * pointwise and vertical-column algebra.  Sizes: E members, J x I grid,
+ * K levels; 3-D arrays (R)[E][J][I][K], 2-D (R)[E][J][I].  Basic-state
+ * arrays carry no member axis.
+ * ==========================================================================*/
+typedef struct lbm_tend_grid_args {
+  int nmem, nlat, nlon, kmax, strictly_linear;
+  double kappa, epsvt, rair;
+  /* vertical constants (R)[K] (sigm: [K+1]) */
+  const void *dsig, *sigm, *alpha, *w3, *wP, *cpg, *sig, *ww, *tmtx, *tref;
+  /* basic state: 3-D (R)[J][I][K], sdot (R)[J][I][K+1], 2-D (R)[J][I] */
+  const void *ub, *vb, *tb, *qb, *tvb, *absvor, *divb, *x5b, *sdotb;
+  const void *pixb, *piyb, *psb;
+  /* perturbation inputs */
+  const void *u, *v, *t, *q, *vor, *div, *pix, *piy, *ps;
+  /* optional grid forcings (NULL = none), member stride in elements */
+  const void *frc_t, *frc_ps, *frc_q;
+  int64_t frc_t_stride, frc_ps_stride, frc_q_stride;
+  /* outputs: 3-D (R)[E][J][I][K], 2-D (R)[E][J][I]; omega may be NULL */
+  void *fu, *fv, *ke, *gt, *xu, *xv, *g, *yu, *yv, *gt_pi, *omega, *sdot;
+} lbm_tend_grid_args;
+
+int lbm_tendency_grid(int prec, const lbm_tend_grid_args* a, void* stream);
+
+/* ============================================================================
+ * Semi-implicit leapfrog update  (Integrator.step, integrator.py:264-315) on
+ * the rectangle spectral layout (R, complex)[E][M][M][K] ((E)[M][M] for pi).
+ * ==========================================================================*/
+typedef struct lbm_implicit_args {
+  int nmem, nmax, kmax;
+  double dt;
+  /* operators (R): lap[M]; kv, kd, ktt, kq [M][K]; ww, tmtx [K][K]; gg,
+   * dsig [K]; minv [M][K][K]; vdiff minv [K][K] or NULL per variable */
+  const void *lap, *kv, *kd, *ktt, *kq, *ww, *tmtx, *gg, *dsig, *minv;
+  const void *vd_vor, *vd_div, *vd_t, *vd_q;
+  /* previous level and explicit tendencies */
+  const void *p_vor, *p_div, *p_t, *p_pi, *p_q;
+  const void *w_vor, *w_div, *w_t, *w_pi, *w_q;
+  /* new level (outputs) */
+  void *n_vor, *n_div, *n_t, *n_pi, *n_q;
+} lbm_implicit_args;
+
+int lbm_implicit_step(int prec, const lbm_implicit_args* a, void* stream);
+
+/* ============================================================================
+ * Fused ensemble stepper (the hot path).  The prognostic state lives in
+ * packed spectral space; each step runs four kernels: grid-point tendency
+ * (with the longitude FFTs), Legendre analysis, implicit spectral update with
+ * the Robert-Asselin filter, Legendre synthesis.  All arrays (R).
+ *
+ * Layouts (E members, J lats, I lons, K levels, M = nmax+1, NS packed):
+ *   sa3  [E][4][NS][K] cplx  current level (t): vor, div, T, q
+ *   sas  [E][4][NS]    cplx  current level surface: pi, and the sigma-weighted
+ *                             column sums of psi, chi, div (for sigma-dot)
+ *   sb3  [E][4][NS][K] cplx  previous level (t - dt), Robert-Asselin filtered
+ *   psa  [E][J][I]           grid ps' of the level before the current one
+ *   psb  [E][J][I]           grid ps' of the filtered previous level
+ *   sf   [E][M][J][K][6] cplx  synthesis (Fourier) of u cos, v cos, vor, div, T, q
+ *   sfs  [E][M][J][5] cplx     pi, H pi, column-sum u cos, v cos, div
+ *   af   [E][M][J][K][7] cplx  weighted Fourier inputs of the analysis
+ *   afs  [E][M][J][2] cplx     gt_pi, pi(t-dt)
+ *   tend [E][4][NS][K] cplx, tends [E][2][NS] cplx   explicit tendencies
+ *   symp, symh [NS][J/2]       P and H at the northern latitudes, packed rows
+ *   tw [I] cplx; jfac [4][J]: gw, gwdel*coslat, 1/(a coslat), coslat
+ *   vert [16][K+1]: see LBM_VERT_* below
+ *   b3 [10][J][K][I]: ub vb tb qb tvb absvor divb x5b tdev tvdev
+ *   bsd [J][K+1][I] basic sigma-dot; b2 [5][J][I]: pixb piyb psbar
+ *                   sum_k dsig ub, sum_k dsig vb
+ *   ops: lap, invlap, nn1a [M]; kv kd ktt kq [M][K]; ww tmtx [K][K];
+ *        minv [nsets][M][K][K] (stored transposed: [n][l][k]);
+ *        vdiff [nsets][4][K][K] (transposed) with vd_on[4] flags
+ *   frc3 [Ef][4][NS][K], frcs [Ef][NS]: spectral forcing (NULL = none),
+ *        Ef = E or 1 (frc_shared = 1)
+ *   err [1] int: set nonzero when a non-finite value is produced
+ * ==========================================================================*/
+enum {
+  LBM_VERT_DSIG = 0, LBM_VERT_SIGM, LBM_VERT_ALPHA, LBM_VERT_W3, LBM_VERT_WP,
+  LBM_VERT_RCPG, LBM_VERT_RDLOG3, LBM_VERT_RALPHA, LBM_VERT_TREF,
+  LBM_VERT_KTREF, LBM_VERT_SIG, LBM_VERT_GG, LBM_VERT_COUNT
+};
+
+typedef struct lbm_stepper_desc {
+  int prec, nmem, nlat, nlon, nmax, kmax, nsets, strictly_linear;
+  int vd_on[4];
+  int frc_shared;
+  double kappa, epsvt, robert;
+  const void *symp, *symh, *tw, *jfac, *vert, *b3, *bsd, *b2;
+  const void *lap, *invlap, *nn1a, *kv, *kd, *ktt, *kq, *ww, *tmtx, *minv, *vdiff;
+  const void *frc3, *frcs;
+  void *sa3, *sas, *sb3, *psa, *psb;
+  void *sf, *sfs, *af, *afs, *tend, *tends;
+  int* err;
+} lbm_stepper_desc;
+
+/* Per-step control.  dt: time step of this call; set: which operator set
+ * (minv/vdiff) matches dt; ps_mode: how the grid ps of the filtered previous
+ * level is brought up to date before this step (0 = already current, 1 =
+ * copy of the current level as in a forward start, 2 = Robert-Asselin
+ * filter); ra_mode: spectral update of the previous level at the end of the
+ * step (0 = copy of the current level, 1 = Robert-Asselin filter). */
+typedef struct lbm_step_ctl {
+  double dt;
+  int set, ps_mode, ra_mode, pad;
+} lbm_step_ctl;
+
+/* Synthesis of the current level into sf/sfs (run once after loading a
+ * state, before the first step). */
+int lbm_stepper_prime(const lbm_stepper_desc* d, void* stream);
+
+/* nsteps steps, one lbm_step_ctl each (host array). */
+int lbm_stepper_run(const lbm_stepper_desc* d, const lbm_step_ctl* ctl,
+                    int nsteps, void* stream);
+
+/* One kernel of one step, for per-kernel timing and profiling: kernel 0 =
+ * grid-point tendency with the longitude FFTs, 1 = Legendre analysis,
+ * 2 = implicit update, 3 = Legendre synthesis.  Launching 0..3 in order is
+ * the same as lbm_stepper_run for that step. */
+int lbm_stepper_launch(const lbm_stepper_desc* d, const lbm_step_ctl* ctl,
+                       int kernel, void* stream);
+
+/* Apply the pending grid-ps update (ps_mode as in lbm_step_ctl) so that psa
+ * holds ps' of the current level and psb that of the filtered previous
+ * level, as after the reference's loop body. */
+int lbm_stepper_flush(const lbm_stepper_desc* d, int ps_mode, void* stream);
+
+/* Column sums of the current level's psi, chi, div into sas[1..3] (needed
+ * after loading a state into sa3). */
+int lbm_stepper_colsum(const lbm_stepper_desc* d, void* stream);
+
+/* CUDA graph of nsteps steps captured from lbm_stepper_run on `stream`
+ * (capture mode global); launch replays it on any stream.  The handle owns
+ * the instantiated graph. */
+typedef struct lbm_graph lbm_graph;
+int lbm_graph_capture(const lbm_stepper_desc* d, const lbm_step_ctl* ctl,
+                      int nsteps, void* stream, lbm_graph** out);
+int lbm_graph_launch(lbm_graph* g, void* stream);
+int lbm_graph_destroy(lbm_graph* g);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LBM_GB300_H */

@@ -1,0 +1,162 @@
+"""Linearised primitive-equation tendencies (drop-in for pylbm_isca/dynamics.py).
+
+``Dynamics.tendencies`` keeps the reference's signature and return value
+(five spectral tendencies, dynamics.py:156-271).  The transforms are the
+lbm_gb300 transform kernels and the whole grid-point part -- column sums,
+sigma-dot, virtual temperature, Simmons-Burridge omega factor, adiabatic and
+advection terms, pressure gradient, vertical advection, hydrostatic and
+energy-conversion operators, kinetic energy, omega diagnostic -- is one
+fused launch of ``lbm_tendency_grid``.  The fused ensemble stepper runs the
+same algebra inside its own grid kernel; this class is the reference-layout
+entry point (used directly by callers and for a forward start from an
+arbitrary grid state).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import TendGridArgs, check, lib, ptr
+from .backend import to_device, stream_handle
+from .constants import EPSVT, KAPPA, OMEGA, RAIR
+
+
+def _column_sum(x, dsig):
+    """S[k] = sum_{l>=k} dsig_l x_l, trailing zero (dynamics.py:96-102)."""
+    w = x * dsig
+    out = torch.zeros(x.shape[:-1] + (x.shape[-1] + 1,), dtype=x.dtype, device=x.device)
+    out[..., :-1] = torch.flip(torch.cumsum(torch.flip(w, (-1,)), -1), (-1,))
+    return out
+
+
+def _sigma_dot(ssum, sigm):
+    """dynamics.py:105-114."""
+    sd = sigm * ssum[..., :1] - ssum
+    sd[..., 0] = 0.0
+    sd[..., -1] = 0.0
+    return sd
+
+
+def _vert_advect(field, sdot, dsig):
+    """dynamics.py:117-143 (used for the time-constant basic state only)."""
+    K = field.shape[-1]
+    lead = torch.broadcast_shapes(field.shape[:-1], sdot.shape[:-1])
+    flux = torch.zeros(lead + (K + 1,), dtype=field.dtype, device=field.device)
+    flux[..., 1:K] = sdot[..., 1:K] * 0.5 * (field[..., 1:K] + field[..., :K - 1])
+    dsdot = sdot[..., 1:] - sdot[..., :-1]
+    return (flux[..., 1:] - flux[..., :-1] - field * dsdot) / dsig
+
+
+class BasicStateTerms:
+    """Basic-state derived fields (dynamics.py:51-93); one-off setup."""
+
+    def __init__(self, sp, vgrid, bs):
+        self.sp, self.vg = sp, vgrid
+        dev = sp.device
+        self.xp = torch
+        self.u = to_device(bs.u, dev)
+        self.v = to_device(bs.v, dev)
+        self.t = to_device(bs.t, dev)
+        self.q = to_device(bs.q, dev)
+        self.ps = to_device(bs.ps, dev)
+        self.coriol = torch.as_tensor((2.0 * OMEGA * sp.mu)[:, None], device=dev)
+        self.vor, self.div_s = sp.uv_to_vordiv(self.u, self.v)
+        self.vor_g = sp.wave_to_grid(self.vor)
+        self.div = sp.wave_to_grid(self.div_s)
+        self.lnps = torch.log(self.ps)
+        self.pix, self.piy = sp.hgrad(sp.grid_to_wave(self.lnps))
+        self.tv = self.t * (1.0 + EPSVT * self.q)
+        self.padv = self.u * self.pix[..., None] + self.v * self.piy[..., None]
+        self.ssum = _column_sum(self.div + self.padv, vgrid.dsig)
+        self.sdot = _sigma_dot(self.ssum, vgrid.sigm)
+        self.x5 = (vgrid.w3 * self.ssum[..., 1:] + vgrid.alpha * self.div
+                   + vgrid.wP * self.padv)
+        from .vertical import compute_tbar
+        vgrid.set_reference_temperature(compute_tbar(self.tv))
+        self.absvor = (self.vor_g + self.coriol[..., None]).contiguous()
+
+
+class Dynamics:
+    """Explicit (non-gravity-wave) tendencies (dynamics.py:146-271)."""
+
+    def __init__(self, sp, vgrid, bst, strictly_linear=False):
+        self.sp, self.vg, self.bs = sp, vgrid, bst
+        self.strictly_linear = bool(strictly_linear)
+        self.diag = {}
+
+    def _grid_kernel(self, st, vor, div, pix, piy, frc_t, frc_ps, frc_q, want_omega=True):
+        sp, vg, bs = self.sp, self.vg, self.bs
+        dev = sp.device
+        u, v = st.u.contiguous(), st.v.contiguous()
+        batched = u.dim() == 4
+        E = u.shape[0] if batched else 1
+        J, I, K = sp.nlat, sp.nlon, vg.kmax
+        f64 = dict(device=dev, dtype=torch.float64)
+        shp3 = u.shape
+        shp2 = shp3[:-1]
+        out = {k: torch.empty(shp3, **f64) for k in
+               ("fu", "fv", "ke", "gt", "xu", "xv", "g", "yu", "yv")}
+        out["gt_pi"] = torch.empty(shp2, **f64)
+        out["omega"] = torch.empty(shp3, **f64) if want_omega else None
+        out["sdot"] = torch.empty(shp2 + (K + 1,), **f64)
+        keep = []
+
+        def c(x):
+            t = x.contiguous()
+            keep.append(t)
+            return ptr(t)
+
+        def frc(x, full_shape):
+            if x is None:
+                return None, 0
+            t = to_device(x, dev).contiguous()
+            keep.append(t)
+            per = int(np.prod(full_shape[1:])) if batched else 0
+            stride = per if (batched and t.dim() == len(full_shape)) else 0
+            return ptr(t), stride
+
+        a = TendGridArgs()
+        a.nmem, a.nlat, a.nlon, a.kmax = E, J, I, K
+        a.strictly_linear = int(self.strictly_linear)
+        a.kappa, a.epsvt, a.rair = KAPPA, EPSVT, RAIR
+        tref = vg.tbar
+        a.dsig, a.sigm, a.alpha, a.w3, a.wP = (c(vg.dsig), c(vg.sigm), c(vg.alpha), c(vg.w3),
+                                               c(vg.wP))
+        a.cpg, a.sig, a.ww, a.tmtx, a.tref = c(vg.cpg), c(vg.sig), c(vg.ww), c(vg.tmtx), c(tref)
+        a.ub, a.vb, a.tb, a.qb, a.tvb = c(bs.u), c(bs.v), c(bs.t), c(bs.q), c(bs.tv)
+        a.absvor, a.divb, a.x5b, a.sdotb = c(bs.absvor), c(bs.div), c(bs.x5), c(bs.sdot)
+        a.pixb, a.piyb, a.psb = c(bs.pix), c(bs.piy), c(bs.ps)
+        a.u, a.v, a.t, a.q = c(u), c(v), c(st.t), c(st.q)
+        a.vor, a.div, a.pix, a.piy, a.ps = c(vor), c(div), c(pix), c(piy), c(st.ps)
+        a.frc_t, a.frc_t_stride = frc(frc_t, shp3)
+        a.frc_ps, a.frc_ps_stride = frc(frc_ps, shp2)
+        a.frc_q, a.frc_q_stride = frc(frc_q, shp3)
+        for k in ("fu", "fv", "ke", "gt", "xu", "xv", "g", "yu", "yv", "gt_pi", "omega", "sdot"):
+            setattr(a, k, ptr(out[k]))
+        check(lib().lbm_tendency_grid(_lib.LBM_F64, a, stream_handle()), "lbm_tendency_grid")
+        return out
+
+    def tendencies(self, st, frc_t=None, frc_vor=None, frc_div=None, frc_ps=None,
+                   frc_q=None):
+        """Explicit tendencies of (vor, div, T, pi, q) in spectral space."""
+        sp = self.sp
+        vor_s, div_s = sp.uv_to_vordiv(st.u, st.v)
+        vor = sp.wave_to_grid(vor_s)
+        div = sp.wave_to_grid(div_s)
+        pi = st.lnps_pert()
+        pix, piy = sp.hgrad(sp.grid_to_wave(pi))
+        o = self._grid_kernel(st, vor, div, pix, piy, frc_t, frc_ps, frc_q)
+        wt_pi = sp.grid_to_wave(o["gt_pi"])
+        wt_t = sp.neg_divergence(o["xu"], o["xv"]) + sp.grid_to_wave(o["gt"])
+        wt_vor, wt_div = sp.uv_to_vordiv(o["fu"], o["fv"])
+        wt_div = wt_div - sp.laplacian(sp.grid_to_wave(o["ke"]))
+        if frc_vor is not None:
+            wt_vor = wt_vor + sp.grid_to_wave(frc_vor)
+        if frc_div is not None:
+            wt_div = wt_div + sp.grid_to_wave(frc_div)
+        wt_q = sp.neg_divergence(o["yu"], o["yv"]) + sp.grid_to_wave(o["g"])
+        self.diag = {"vor": vor, "div": div, "vor_s": vor_s, "div_s": div_s,
+                     "omega": o["omega"], "sdot": o["sdot"], "pi": pi}
+        return wt_vor, wt_div, wt_t, wt_pi, wt_q

@@ -1,0 +1,331 @@
+"""Host driver of the fused ensemble stepper (lbm_stepper_* in the C ABI).
+
+The stepper owns the packed spectral state of E members and every operator
+the four step kernels read, in the working precision (FP64 or FP32).  Setup
+quantities (Legendre tables, Gauss weights, semi-implicit inverses) are
+produced in FP64 by the library's setup kernels and rounded once.
+
+Step bookkeeping follows model.py:213-247: a step carries its dt (the
+start-up calls use delt/2^(inistp-istep+1)), whether the previous level is
+set by copy (forward start) or by the Robert-Asselin filter, and how the
+grid ps of the previous level is brought up to date (the ps part of the
+filter is applied at the top of the next step, once ps(t+dt) exists in grid
+space).  Runs of identical steady-state steps are captured once into a CUDA
+graph (lbm_graph_capture) and replayed.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import StepCtl, StepperDesc, check, lib, ptr
+from .backend import stream_handle
+from .constants import EPSVT, KAPPA, RAIR
+
+VERT_ROWS = 12   # LBM_VERT_COUNT in include/lbm_gb300.h
+
+
+class EnsembleStepper:
+    """Fused GPU time stepping of `nmem` members sharing one basic state."""
+
+    def __init__(self, sp, vg, bst, damping, semi, vdiff, nmem, precision="fp64",
+                 robert=0.04, strictly_linear=False, stream=None):
+        if precision not in ("fp64", "fp32"):
+            raise ValueError("precision must be 'fp64' or 'fp32'")
+        self.sp, self.vg, self.bst = sp, vg, bst
+        self.semi, self.vdiff = semi, vdiff
+        self.dev = dev = sp.device
+        self.precision = precision
+        self.rd = torch.float64 if precision == "fp64" else torch.float32
+        self.cd = torch.complex128 if precision == "fp64" else torch.complex64
+        self.prec_id = _lib.LBM_F64 if precision == "fp64" else _lib.LBM_F32
+        self.E = E = int(nmem)
+        self.N = N = sp.nmax
+        self.M = M = N + 1
+        self.J, self.I, self.K = J, I, K = sp.nlat, sp.nlon, vg.kmax
+        self.NS = NS = M * (M + 1) // 2
+        self.stream = stream if stream is not None else torch.cuda.Stream(device=dev)
+        rd, cd = self.rd, self.cd
+        mm, nn = np.nonzero(np.triu(np.ones((M, M), dtype=bool)))
+        self.pm = torch.as_tensor(mm, device=dev)
+        self.pn = torch.as_tensor(nn, device=dev)
+        R = lambda x: x.to(device=dev, dtype=rd).contiguous()   # noqa: E731
+        JH = J // 2
+        self.symp = R(sp.pnm[self.pm, self.pn, :JH])
+        self.symh = R(sp.hnm[self.pm, self.pn, :JH])
+        self.tw = R(sp._tw64)
+        coslat = sp.coslat
+        gwdel = torch.as_tensor(sp.gwdel, device=dev)
+        self.jfac = R(torch.stack([torch.as_tensor(sp.gw, device=dev), gwdel * coslat,
+                                   1.0 / (sp.a * coslat), coslat]))
+        vh = vg.host
+        vert = np.zeros((VERT_ROWS, K + 1))
+        vert[0, :K] = vh("dsig")
+        vert[1, :] = vh("sigm")
+        vert[2, :K] = vh("alpha")
+        vert[3, :K] = vh("w3")
+        vert[4, :K] = vh("wP")
+        vert[5, :K] = RAIR * vh("cpg")
+        vert[6, :K] = RAIR * vh("dlog3")
+        vert[7, :K] = RAIR * vh("alpha")
+        vert[8, :K] = vh("tbar")
+        vert[9, :K] = KAPPA * vh("tbar")
+        vert[10, :K] = vh("sig")
+        vert[11, :K] = vh("gg")
+        self.vert = R(torch.as_tensor(vert))
+        tref = torch.as_tensor(vh("tbar"), device=dev)
+        b = bst
+        f3 = [b.u, b.v, b.t, b.q, b.tv, b.absvor, b.div, b.x5, b.t - tref, b.tv - tref]
+        self.b3 = R(torch.stack([x.permute(0, 2, 1) for x in f3]))        # [10][J][K][I]
+        self.bsd = R(b.sdot.permute(0, 2, 1))                             # [J][K+1][I]
+        dsig = torch.as_tensor(vh("dsig"), device=dev)
+        self.b2 = R(torch.stack([b.pix, b.piy, b.ps, (b.u * dsig).sum(-1),
+                                 (b.v * dsig).sum(-1)]))                  # [5][J][I]
+        self.lap = R(sp.laplace)
+        self.invlap = R(sp.inv_laplace)
+        self.nn1a = R(-sp.laplace)
+        self.kv, self.kd = R(damping.kv), R(damping.kd)
+        self.ktt, self.kq = R(damping.ktt), R(damping.kq)
+        self.ww = R(torch.as_tensor(vh("ww")))
+        self.tmtx = R(torch.as_tensor(vh("tmtx")))
+        self.robert = float(robert)
+        self.strictly_linear = int(bool(strictly_linear))
+        self.vd_on = [int(vdiff.coef[n] is not None) for n in ("vor", "div", "t", "q")]
+        # state and intermediates
+        z = lambda *s: torch.zeros(s, device=dev, dtype=cd)   # noqa: E731
+        self.sa3, self.sas, self.sb3 = z(E, 4, NS, K), z(E, 4, NS), z(E, 4, NS, K)
+        self.psa = torch.zeros((E, J, I), device=dev, dtype=rd)
+        self.psb = torch.zeros((E, J, I), device=dev, dtype=rd)
+        self.sf, self.sfs = z(E, M, J, K, 6), z(E, M, J, 5)
+        self.af, self.afs = z(E, M, J, K, 7), z(E, M, J, 2)
+        self.tend, self.tends = z(E, 4, NS, K), z(E, 2, NS)
+        self.err = torch.zeros(1, device=dev, dtype=torch.int32)
+        self.frc3 = self.frcs = None
+        self.frc_shared = 1
+        self._dts = []
+        self.minv = self.vdm = None
+        self._graphs = {}
+        self.pending_ps_mode = 0
+        self._desc = None
+
+    # ------------------------------------------------------------------
+    def set_timesteps(self, dts):
+        """Operator sets (semi-implicit inverse, vertical diffusion) per dt."""
+        dts = [float(x) for x in dts]
+        if dts == self._dts:
+            return
+        K, M = self.K, self.M
+        mins, vds = [], []
+        for dt in dts:
+            _, minv, _ = self.semi.matrices(dt)
+            mins.append(minv.transpose(1, 2))                    # stored (n, l, k)
+            ops = self.vdiff.operators(dt)
+            eye = torch.eye(K, device=self.dev, dtype=torch.float64)
+            vds.append(torch.stack([(ops[n] if ops[n] is not None else eye).T
+                                    for n in ("vor", "div", "t", "q")]))
+        self.minv = torch.stack(mins).to(self.rd).contiguous()   # [nsets][M][K][K]
+        self.vdm = torch.stack(vds).to(self.rd).contiguous()     # [nsets][4][K][K]
+        self._dts = dts
+        self._drop_graphs()
+        self._desc = None
+
+    def set_index(self, dt):
+        return self._dts.index(float(dt))
+
+    def set_forcing(self, frc_vor=None, frc_div=None, frc_t=None, frc_pi=None, frc_q=None,
+                    per_member=False):
+        """Spectral forcings, rectangle layout ((E,) M, M, K) / ((E,) M, M)."""
+        if all(x is None for x in (frc_vor, frc_div, frc_t, frc_pi, frc_q)):
+            self.frc3 = self.frcs = None
+            self.frc_shared = 1
+            self._desc = None
+            self._drop_graphs()
+            return
+        Ef = self.E if per_member else 1
+        f3 = torch.zeros((Ef, 4, self.NS, self.K), device=self.dev, dtype=self.cd)
+        fs = torch.zeros((Ef, self.NS), device=self.dev, dtype=self.cd)
+        for i, x in enumerate((frc_vor, frc_div, frc_t, frc_q)):
+            if x is not None:           # (B, M, M, K), B = 1 or E
+                p = self.pack(x).reshape(-1, self.NS, self.K)
+                f3[:, i] = p.expand(Ef, self.NS, self.K)
+        if frc_pi is not None:          # (B, M, M)
+            p = self.pack(frc_pi).reshape(-1, self.NS)
+            fs[:] = p.expand(Ef, self.NS)
+        new_ptrs = self.frc3 is None
+        if self.frc3 is not None and self.frc3.shape == f3.shape:
+            self.frc3.copy_(f3)
+            self.frcs.copy_(fs)
+        else:
+            self.frc3, self.frcs = f3, fs
+            new_ptrs = True
+        self.frc_shared = 0 if per_member else 1
+        if new_ptrs:
+            self._desc = None
+            self._drop_graphs()
+
+    # ------------------------------------------------------------------
+    def pack(self, x):
+        """(..., M, M[, K]) rectangle -> (..., NS[, K]) packed, working precision."""
+        x = x.to(self.dev)
+        if x.shape[-2:] == (self.M, self.M):
+            return x[..., self.pm, self.pn].to(self.cd)
+        return x[..., self.pm, self.pn, :].to(self.cd)
+
+    def unpack(self, p, has_k=True):
+        lead = p.shape[:-2] if has_k else p.shape[:-1]
+        shape = lead + (self.M, self.M) + ((p.shape[-1],) if has_k else ())
+        out = torch.zeros(shape, device=self.dev, dtype=torch.complex128)
+        if has_k:
+            out[..., self.pm, self.pn, :] = p.to(torch.complex128)
+        else:
+            out[..., self.pm, self.pn] = p.to(torch.complex128)
+        return out
+
+    def load(self, a_spec, b_spec, psa, psb):
+        """Load the current level (spectral dict incl. pi), the previous level
+        (spectral vor/div/t/q) and both grid ps' fields; member axis first."""
+        for i, k in enumerate(("vor", "div", "t", "q")):
+            self.sa3[:, i] = self.pack(a_spec[k]).reshape(self.E, self.NS, self.K)
+            self.sb3[:, i] = self.pack(b_spec[k]).reshape(self.E, self.NS, self.K)
+        self.sas[:, 0] = self.pack(a_spec["pi"]).reshape(self.E, self.NS)
+        self.psa.copy_(psa.reshape(self.E, self.J, self.I))
+        self.psb.copy_(psb.reshape(self.E, self.J, self.I))
+        self.pending_ps_mode = 0
+        self.err.zero_()
+        with torch.cuda.stream(self.stream):
+            torch.cuda.current_stream().wait_stream(torch.cuda.default_stream(self.dev))
+            d = self.desc()
+            check(lib().lbm_stepper_colsum(C.byref(d), stream_handle(self.stream)),
+                  "lbm_stepper_colsum")
+            check(lib().lbm_stepper_prime(C.byref(d), stream_handle(self.stream)),
+                  "lbm_stepper_prime")
+
+    def desc(self):
+        if self._desc is not None:
+            return self._desc
+        d = StepperDesc()
+        d.prec = self.prec_id
+        d.nmem, d.nlat, d.nlon, d.nmax, d.kmax = self.E, self.J, self.I, self.N, self.K
+        d.nsets = len(self._dts)
+        d.strictly_linear = self.strictly_linear
+        for i in range(4):
+            d.vd_on[i] = self.vd_on[i]
+        d.frc_shared = self.frc_shared
+        d.kappa, d.epsvt, d.robert = KAPPA, EPSVT, self.robert
+        for name in ("symp", "symh", "tw", "jfac", "vert", "b3", "bsd", "b2", "lap", "invlap",
+                     "nn1a", "kv", "kd", "ktt", "kq", "ww", "tmtx", "sa3", "sas", "sb3", "psa",
+                     "psb", "sf", "sfs", "af", "afs", "tend", "tends"):
+            setattr(d, name, ptr(getattr(self, name)))
+        d.minv = ptr(self.minv)
+        d.vdiff = ptr(self.vdm)
+        d.frc3 = ptr(self.frc3)
+        d.frcs = ptr(self.frcs)
+        d.err = C.cast(C.c_void_p(self.err.data_ptr()), C.POINTER(C.c_int))
+        self._desc = d
+        return d
+
+    # ------------------------------------------------------------------
+    def _ctl(self, steps):
+        arr = (StepCtl * len(steps))()
+        for i, (dt, start, psm) in enumerate(steps):
+            arr[i].dt = float(dt)
+            arr[i].set = self.set_index(dt)
+            arr[i].ps_mode = psm
+            arr[i].ra_mode = 0 if start else 1
+        return arr
+
+    def plan(self, steps):
+        """[(dt, start)] -> [(dt, start, ps_mode)] continuing from the current
+        pending ps update."""
+        out = []
+        pend = self.pending_ps_mode
+        for dt, start in steps:
+            out.append((dt, start, pend))
+            pend = 1 if start else 2
+        return out, pend
+
+    def run(self, steps, use_graph=True, graph_chunk=72):
+        """Advance through `steps` = [(dt, is_start_step), ...]."""
+        planned, pend = self.plan(steps)
+        s = stream_handle(self.stream)
+        L = lib()
+        self.stream.wait_stream(torch.cuda.default_stream(self.dev))
+        with torch.cuda.stream(self.stream):
+            d = self.desc()
+            i = 0
+            while i < len(planned):
+                dt, start, psm = planned[i]
+                steady = (not start) and psm == 2
+                j = i
+                while j < len(planned) and planned[j] == planned[i]:
+                    j += 1
+                n_same = j - i
+                if use_graph and steady and n_same >= 2:
+                    n = min(n_same, graph_chunk)
+                    g = self._graph(planned[i:i + n])
+                    check(L.lbm_graph_launch(g, s), "lbm_graph_launch")
+                    i += n
+                else:
+                    ctl = self._ctl(planned[i:i + 1])
+                    check(L.lbm_stepper_run(C.byref(d), ctl, 1, s), "lbm_stepper_run")
+                    i += 1
+        self.pending_ps_mode = pend
+
+    def _graph(self, planned):
+        key = (len(planned),) + planned[0]
+        g = self._graphs.get(key)
+        if g is None:
+            ctl = self._ctl(planned)
+            h = C.c_void_p()
+            check(lib().lbm_graph_capture(C.byref(self.desc()), ctl, len(planned),
+                                          stream_handle(self.stream), C.byref(h)),
+                  "lbm_graph_capture")
+            g = h
+            self._graphs[key] = g
+        return g
+
+    def _drop_graphs(self):
+        for g in self._graphs.values():
+            lib().lbm_graph_destroy(g)
+        self._graphs = {}
+
+    def flush(self):
+        """Bring psa/psb up to date with the last step."""
+        if self.pending_ps_mode == 0:
+            return
+        self.stream.wait_stream(torch.cuda.default_stream(self.dev))
+        with torch.cuda.stream(self.stream):
+            check(lib().lbm_stepper_flush(C.byref(self.desc()), self.pending_ps_mode,
+                                          stream_handle(self.stream)), "lbm_stepper_flush")
+        self.pending_ps_mode = 0
+
+    def check_finite(self):
+        self.stream.synchronize()
+        return int(self.err.item()) == 0
+
+    def snapshot(self):
+        """Copy of the current level (rectangle dict incl. pi)."""
+        torch.cuda.default_stream(self.dev).wait_stream(self.stream)
+        a = {k: self.unpack(self.sa3[:, i]) for i, k in enumerate(("vor", "div", "t", "q"))}
+        a["pi"] = self.unpack(self.sas[:, 0], has_k=False)
+        return a
+
+    def spectral_state(self):
+        """Current (a) and previous (b) levels as rectangle dicts (complex128)."""
+        torch.cuda.default_stream(self.dev).wait_stream(self.stream)
+        a, b = {}, {}
+        for i, k in enumerate(("vor", "div", "t", "q")):
+            a[k] = self.unpack(self.sa3[:, i])
+            b[k] = self.unpack(self.sb3[:, i])
+        a["pi"] = self.unpack(self.sas[:, 0], has_k=False)
+        return a, b
+
+    def __del__(self):
+        try:
+            self._drop_graphs()
+        except Exception:
+            pass

@@ -1,0 +1,43 @@
+"""The C-ABI library builds, loads and exports every entry point that
+include/lbm_gb300.h declares (no compute calls: runs without a GPU)."""
+
+import ctypes
+import os
+import re
+
+from conftest import ROOT
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "lbm_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = set(re.findall(r"\b(lbm_[a-z0-9_]+)\s*\(", src))
+    return sorted(names)
+
+
+def test_header_declares_the_entry_points():
+    names = declared_symbols()
+    for must in ("lbm_legendre_tables", "lbm_fourier_forward", "lbm_tendency_grid",
+                 "lbm_implicit_step", "lbm_stepper_run", "lbm_graph_capture"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    from lbm_isca_gb300.build import build
+    path = build()
+    lib = ctypes.CDLL(path)
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+    lib.lbm_version.restype = ctypes.c_char_p
+    assert lib.lbm_version().startswith(b"lbm_gb300")
+
+
+def test_bad_arguments_are_rejected_without_a_device():
+    """Argument validation happens before any CUDA call."""
+    from lbm_isca_gb300 import _lib
+    L = _lib.lib()
+    assert L.lbm_gauss_legendre(1, None, None, None) == _lib.LBM_ERR_ARG
+    assert L.lbm_fourier_forward(_lib.LBM_F64, 1, 32, 100, 1, 21, None, None, None, None,
+                                 None) == _lib.LBM_ERR_ARG
+    assert L.lbm_stepper_run(None, None, 1, None) == _lib.LBM_ERR_ARG
+    assert L.lbm_batched_inverse(1, 65, None, None, None, None) == _lib.LBM_ERR_ARG
