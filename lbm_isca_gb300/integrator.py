@@ -213,8 +213,12 @@ class Integrator:
         self.semi.prepare(dt)
         self.vdiff.prepare(dt)
         keys = ("vor", "div", "t", "pi", "q")
-        pv = {k: prev[k].to(torch.complex128).contiguous() for k in keys}
-        tv = dict(zip(keys, (x.to(torch.complex128).contiguous() for x in tend)))
+
+        def dev(x):
+            t = x if isinstance(x, torch.Tensor) else torch.as_tensor(np.asarray(x))
+            return t.to(device=sp.device, dtype=torch.complex128).contiguous()
+        pv = {k: dev(prev[k]) for k in keys}
+        tv = dict(zip(keys, (dev(x) for x in tend)))
         K = vg.kmax
         batched = pv["vor"].dim() == 4
         E = pv["vor"].shape[0] if batched else 1

@@ -1,0 +1,154 @@
+"""Host-side logic that needs no GPU: step schedule, ps-filter bookkeeping,
+synthetic inputs, device selection, member sharding (2 gloo ranks)."""
+
+import os
+import socket
+import types
+
+import numpy as np
+import pytest
+
+from lbm_isca_gb300 import configs
+from lbm_isca_gb300.sharding import member_block
+
+
+def test_schedule_matches_reference_loop():
+    """model.py:213-219: inistp start-up calls at dt/2^(inistp-istep+1)."""
+    from lbm_isca_gb300.model import LBM, Config
+    fake = types.SimpleNamespace(cfg=Config(delt=1200.0, inistp=2))
+    sched = LBM._schedule(fake, 5)
+    assert sched[:2] == [(300.0, True), (600.0, True)]
+    assert sched[2:] == [(1200.0, False)] * 5
+    fake.cfg.inistp = 0
+    assert LBM._schedule(fake, 3) == [(1200.0, False)] * 3
+
+
+def test_ps_mode_plan():
+    """Grid-ps filter bookkeeping: first step 0, after a start-up call 1
+    (copy), after an advancing call 2 (Robert-Asselin)."""
+    from lbm_isca_gb300.stepper import EnsembleStepper
+    fake = types.SimpleNamespace(pending_ps_mode=0)
+    steps = [(300.0, True), (600.0, True), (1200.0, False), (1200.0, False)]
+    planned, pend = EnsembleStepper.plan(fake, steps)
+    assert [p[2] for p in planned] == [0, 1, 1, 2]
+    assert pend == 2
+    fake.pending_ps_mode = 2
+    planned, pend = EnsembleStepper.plan(fake, [(1200.0, False)])
+    assert planned == [(1200.0, False, 2)] and pend == 2
+
+
+def test_heating_profile_peaks_at_sigma_peak():
+    sig = np.linspace(0.0, 1.0, 100001)
+    for sp in (0.3, 0.45, 0.6):
+        prof = configs.heating_profile(sig, sp)
+        assert abs(sig[np.argmax(prof)] - sp) < 1e-4
+        assert abs(prof[0]) < 1e-12 and abs(prof[-1]) < 1e-12
+
+
+def test_elliptic_heating_and_ensemble_draws():
+    sigm = configs.equal_sigma_half_levels(20)
+    h = configs.elliptic_heating(128, 64, sigm)
+    assert h.shape == (64, 128, 20)
+    assert 0.0 < h.max() <= 2.0 / 86400.0 + 1e-18
+    _, lat = configs.gaussian_latitudes(64)
+    lon = np.arange(128) * 360.0 / 128
+    j, i, _ = np.unravel_index(np.argmax(h), h.shape)
+    assert abs(lat[j]) < 3.0 and abs(lon[i] - 120.0) <= 2.9
+    assert h[np.abs(lat) > 10.0].max() == 0.0           # compact support
+    e1, p1 = configs.ensemble_heating(64, 32, sigm, 3, seed=7)
+    e2, p2 = configs.ensemble_heating(64, 32, sigm, 3, seed=7)
+    assert np.array_equal(e1, e2) and p1 == p2
+    for lon0, lat0, amp, sp in p1:
+        assert 0 <= lon0 < 360 and -15 <= lat0 <= 15 and amp > 0 and 0.3 <= sp <= 0.6
+
+
+def test_solid_body_state_is_balanced_and_monotone():
+    sigm = configs.equal_sigma_half_levels(20)
+    bs = configs.solid_body_basic_state(128, 64, sigm)
+    mu, _ = configs.gaussian_latitudes(64)
+    assert np.allclose(bs.u[:, 0, 0], 15.0 * np.sqrt(1 - mu ** 2))
+    assert bs.v.max() == 0.0 and bs.q.max() == 0.0
+    t = bs.t[0, 0]
+    assert np.all(np.diff(t) <= 0.0) and t.min() >= configs.T_FLOOR
+    assert bs.ps.max() <= configs.PS_EQUATOR_HPA + 1e-9
+
+
+def test_plain_damping_profile():
+    kw = configs.plain_damping(20)
+    assert kw["ddragv"][0] == 1.0 and kw["ddragv"][-1] == 1.0
+    assert kw["ddragv"][1:-1] == [30.0] * 18
+    assert kw["sponge"] is False and kw["vdifv"] is None and kw["hdif_tefold"] == 6.0
+
+
+def test_backend_without_a_gpu():
+    torch = pytest.importorskip("torch")
+    from lbm_isca_gb300.backend import resolve
+    with pytest.raises(ValueError):
+        resolve("tpu")
+    with pytest.raises(RuntimeError):
+        resolve("cpu")
+    if not torch.cuda.is_available():
+        with pytest.raises(RuntimeError):
+            resolve("gb300")
+
+
+def test_member_block_partition():
+    for total in (1, 7, 96, 512):
+        for world in (1, 2, 3, 8):
+            blocks = [member_block(total, world, r) for r in range(world)]
+            assert sum(c for _, c in blocks) == total
+            pos = 0
+            for first, count in blocks:
+                assert first == pos
+                pos += count
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, total, out_dir):
+    """Each rank integrates its member block with the oracle (T21, 6 steps)
+    and the blocks are gathered over gloo."""
+    import torch
+    import torch.distributed as dist
+    from oracle import lbm_oracle as orc
+    from lbm_isca_gb300.sharding import gather_members
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    first, count = member_block(total, world, rank)
+    sigm = configs.equal_sigma_half_levels(20)
+    heats, _ = configs.ensemble_heating(64, 32, sigm, total, seed=3)
+    tr = orc.SphericalTransform(64, 32, 21)
+    lv = orc.SigmaLevels(sigm)
+    bs = configs.solid_body_basic_state(64, 32, sigm)
+    m = orc.OracleModel(tr, lv, bs, orc.RunConfig(**configs.plain_damping(20)), nmem=count)
+    m.run(4, frc_t=heats[first:first + count])
+    local = torch.as_tensor(m.ga.t)
+    full = gather_members(local, world)
+    if rank == 0:
+        np.save(os.path.join(out_dir, "full.npy"), full.numpy())
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_sharded_members_match_single_process(tmp_path):
+    """2 gloo ranks, 3 members split 2 + 1: identical to one 3-member run."""
+    torch = pytest.importorskip("torch")
+    import torch.multiprocessing as tmp
+    port = _free_port()
+    tmp.spawn(_rank_main, args=(2, port, 3, str(tmp_path)), nprocs=2, join=True)
+    full = np.load(os.path.join(tmp_path, "full.npy"))
+    from oracle import lbm_oracle as orc
+    sigm = configs.equal_sigma_half_levels(20)
+    heats, _ = configs.ensemble_heating(64, 32, sigm, 3, seed=3)
+    tr = orc.SphericalTransform(64, 32, 21)
+    lv = orc.SigmaLevels(sigm)
+    bs = configs.solid_body_basic_state(64, 32, sigm)
+    m = orc.OracleModel(tr, lv, bs, orc.RunConfig(**configs.plain_damping(20)), nmem=3)
+    m.run(4, frc_t=heats)
+    assert full.shape == m.ga.t.shape
+    assert np.abs(full - m.ga.t).max() <= 1e-12 * np.abs(m.ga.t).max()
