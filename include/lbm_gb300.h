@@ -191,6 +191,8 @@ int lbm_implicit_step(int prec, const lbm_implicit_args* a, void* stream);
  *   ops: lap, invlap, nn1a [M]; kv kd ktt kq [M][K]; ww tmtx [K][K];
  *        minv [nsets][M][K][K] (stored transposed: [n][l][k]);
  *        vdiff [nsets][4][K][K] (transposed) with vd_on[4] flags
+ *   dft [M][I/4+1] (cos, sin)(2 pi m i / I): longitude DFT table of the FP32
+ *        grid kernel (may be NULL in FP64 mode)
  *   frc3 [Ef][4][NS][K], frcs [Ef][NS]: spectral forcing (NULL = none),
  *        Ef = E or 1 (frc_shared = 1)
  *   err [1] int: set nonzero when a non-finite value is produced
@@ -208,7 +210,7 @@ typedef struct lbm_stepper_desc {
   double kappa, epsvt, robert;
   const void *symp, *symh, *tw, *jfac, *vert, *b3, *bsd, *b2;
   const void *lap, *invlap, *nn1a, *kv, *kd, *ktt, *kq, *ww, *tmtx, *minv, *vdiff;
-  const void *frc3, *frcs;
+  const void *frc3, *frcs, *dft;
   void *sa3, *sas, *sb3, *psa, *psb;
   void *sf, *sfs, *af, *afs, *tend, *tends;
   int* err;

@@ -52,7 +52,7 @@ class StepperDesc(C.Structure):
                    ("kappa", F64), ("epsvt", F64), ("robert", F64)]
                 + [(n, VP) for n in ("symp", "symh", "tw", "jfac", "vert", "b3", "bsd", "b2",
                                      "lap", "invlap", "nn1a", "kv", "kd", "ktt", "kq", "ww",
-                                     "tmtx", "minv", "vdiff", "frc3", "frcs", "sa3", "sas",
+                                     "tmtx", "minv", "vdiff", "frc3", "frcs", "dft", "sa3", "sas",
                                      "sb3", "psa", "psb", "sf", "sfs", "af", "afs", "tend",
                                      "tends")]
                 + [("err", C.POINTER(I32))])

@@ -40,6 +40,7 @@ template <typename R> struct SD {
   const R *jfac, *vert, *b3, *bsd, *b2;
   const R *lap, *invlap, *nn1a, *kv, *kd, *ktt, *kq, *ww, *tmtx, *minv, *vdiff;
   const C2<R> *frc3, *frcs;
+  const float2* dft;
   C2<R> *sa3, *sas, *sb3;
   R *psa, *psb;
   C2<R> *sf, *sfs, *af, *afs, *tend, *tends;
@@ -61,6 +62,7 @@ template <typename R> SD<R> make_sd(const lbm_stepper_desc& d) {
   s.ww = (const R*)d.ww; s.tmtx = (const R*)d.tmtx; s.minv = (const R*)d.minv;
   s.vdiff = (const R*)d.vdiff;
   s.frc3 = (const C2<R>*)d.frc3; s.frcs = (const C2<R>*)d.frcs;
+  s.dft = (const float2*)d.dft;
   s.sa3 = (C2<R>*)d.sa3; s.sas = (C2<R>*)d.sas; s.sb3 = (C2<R>*)d.sb3;
   s.psa = (R*)d.psa; s.psb = (R*)d.psb;
   s.sf = (C2<R>*)d.sf; s.sfs = (C2<R>*)d.sfs; s.af = (C2<R>*)d.af; s.afs = (C2<R>*)d.afs;
@@ -339,7 +341,7 @@ __global__ void __launch_bounds__(NT) k_grid(SD<R> d, int ps_mode) {
 // =============================================================================
 // Legendre analysis: af -> tend, per (member, m-pair, level chunk)
 // =============================================================================
-constexpr int AN_JC = 4;      // latitude pairs staged per pass
+constexpr int AN_JC = 8;      // latitude pairs staged per pass
 
 template <typename R> struct PairRows {
   int m1, m2, L1, L2, NR;
@@ -391,20 +393,21 @@ __global__ void k_anal(SD<R> d) {
     const int jc = min(AN_JC, JH - jh0);
     __syncthreads();
     // stage sym/anti combinations of the 7 inputs
-    for (int idx = tid; idx < nm * jc * kn * AF_N; idx += nt) {
-      const int a = idx % AF_N;
-      int r = idx / AF_N;
-      const int kk = r % kn;
-      r /= kn;
-      const int jj = r % jc, mm = r / jc;
+    // one warp per (m, latitude pair): contiguous runs of kn * 7 values
+    const int nwarp = nt >> 5, wid = tid >> 5, lane = tid & 31;
+    const int rowlen = kn * AF_N;
+    for (int w = wid; w < nm * jc; w += nwarp) {
+      const int mm = w / jc, jj = w - mm * jc;
       const int m = mm ? pr.m2 : pr.m1;
       const int jn = jh0 + jj, js = J - 1 - jn;
-      const size_t base = (size_t)m * J;
-      const C2<R> xn = afe[((base + jn) * K + k0 + kk) * AF_N + a];
-      const C2<R> xsouth = afe[((base + js) * K + k0 + kk) * AF_N + a];
-      C2<R>* dst = xs + ((((size_t)mm * AN_JC + jj) * KC + kk) * AF_N + a) * 2;
-      dst[0] = xn + xsouth;
-      dst[1] = xn - xsouth;
+      const C2<R>* srcn = afe + (((size_t)m * J + jn) * K + k0) * AF_N;
+      const C2<R>* srcs = afe + (((size_t)m * J + js) * K + k0) * AF_N;
+      C2<R>* dst = xs + (((size_t)mm * AN_JC + jj) * KC) * AF_N * 2;
+      for (int c = lane; c < rowlen; c += 32) {
+        const C2<R> xn = srcn[c], xsouth = srcs[c];
+        dst[2 * c] = xn + xsouth;
+        dst[2 * c + 1] = xn - xsouth;
+      }
     }
     __syncthreads();
     if (active) {
@@ -711,11 +714,13 @@ __global__ void k_synth(SD<R> d) {
   const size_t jmK = (size_t)J * K;
   C2<R>* sfe = d.sf + (size_t)e * M * jmK * SF_N;
   const int nm = pr.L2 ? 2 : 1;
-  for (int it = tid; it < nm * NJG * KC; it += nt) {
+  // one (level, latitude group) per item, both m of the pair in turn: every
+  // item walks N + 2 rows, so the pair's rows are balanced across threads
+  for (int it = tid; it < NJG * KC; it += nt) {
     const int kk = it % KC;
-    const int jg = (it / KC) % NJG;
-    const int mm = it / (KC * NJG);
+    const int jg = it / KC;
     if (kk >= kn) continue;
+   for (int mm = 0; mm < nm; ++mm) {
     const int m = mm ? pr.m2 : pr.m1;
     const int rb = mm ? pr.L1 : 0, re = mm ? pr.NR : pr.L1;
     // accumulators: [jg][term][plus/minus]; terms: Pchi Hpsi Ppsi Hchi Pvor Pdiv Pt Pq
@@ -767,6 +772,7 @@ __global__ void k_synth(SD<R> d) {
         o[SF_Q] = comb(7);
       }
     }
+   }
   }
   // surface fields (first level chunk only)
   if (kc != 0) return;
@@ -844,6 +850,10 @@ __global__ void k_ps_flush(SD<R> d, int ps_mode) {
   }
 }
 
+}  // namespace lbm
+#include "grid_dft.cuh"
+namespace lbm {
+
 // ---- launch configuration ------------------------------------------------------
 template <typename R> struct Cfg;
 template <> struct Cfg<float> { static constexpr int NC = 4, KCA = 20, JG = 2, KCS = 20; };
@@ -874,8 +884,14 @@ template <typename R, int I> int launch_step(const SD<R>& d, const lbm_step_ctl&
   const int JH = d.J / 2;
   const int NRmax = d.N + 2;
   const size_t gsm = GridSmem<R, I, KB, NT>::bytes(d.M);
-  if (only < 0 || only == 0)
-    k_grid<R, I, KB, NT><<<dim3(d.J, d.E), NT, gsm, st>>>(d, c.ps_mode);
+  if (only < 0 || only == 0) {
+    if constexpr (sizeof(R) == 4) {
+      const size_t dsm = sizeof(float) * (size_t)DftLayout(I, d.M, d.K, DftGrid<I>::KB).total;
+      k_grid_dft<I><<<dim3(d.J, d.E), DftGrid<I>::NT, dsm, st>>>(d, d.dft, c.ps_mode);
+    } else {
+      k_grid<R, I, KB, NT><<<dim3(d.J, d.E), NT, gsm, st>>>(d, c.ps_mode);
+    }
+  }
   if (only < 0 || only == 1) {
     constexpr int NC = Cfg<R>::NC, KC = Cfg<R>::KCA;
     const int G = (d.N + 2 + NC - 1) / NC + 1;
@@ -892,7 +908,7 @@ template <typename R, int I> int launch_step(const SD<R>& d, const lbm_step_ctl&
   if (only < 0 || only == 3) {
     constexpr int JG = Cfg<R>::JG, KC = Cfg<R>::KCS;
     const int NJG = (JH + JG - 1) / JG;
-    int nt = 2 * NJG * KC;
+    int nt = NJG * KC;
     nt = nt > 512 ? 512 : ((nt + 31) / 32) * 32;
     k_synth<R, JG, KC><<<dim3(NP, d.E, (d.K + KC - 1) / KC), nt, synth_smem<R>(NRmax, JH), st>>>(d);
   }
@@ -903,8 +919,13 @@ template <typename R, int I> int launch_step(const SD<R>& d, const lbm_step_ctl&
 template <typename R, int I> void set_attrs(const SD<R>& d) {
   constexpr int KB = grid_kb<R, I>(), NT = grid_nt<R, I>();
   const int JH = d.J / 2, NRmax = d.N + 2;
-  cudaFuncSetAttribute(k_grid<R, I, KB, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)GridSmem<R, I, KB, NT>::bytes(d.M));
+  if constexpr (sizeof(R) == 4) {
+    cudaFuncSetAttribute(k_grid_dft<I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(sizeof(float) * DftLayout(I, d.M, d.K, DftGrid<I>::KB).total));
+  } else {
+    cudaFuncSetAttribute(k_grid<R, I, KB, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)GridSmem<R, I, KB, NT>::bytes(d.M));
+  }
   size_t sm = anal_smem<R>(NRmax, JH);
   const size_t sm2 = sizeof(R) * 2 * (size_t)NRmax * JH + sizeof(C2<R>) * (size_t)2 * JH * 2 * 2;
   if (sm2 > sm) sm = sm2;
@@ -928,6 +949,10 @@ template <typename R> int validate(const SD<R>& d) {
     return LBM_ERR_ARG;
   for (int f = 0; f < 4; ++f)
     if (d.vd_on[f] && !d.vdiff) return LBM_ERR_ARG;
+  if (sizeof(R) == 4 && !d.dft) return LBM_ERR_ARG;
+  if (sizeof(R) == 4 &&
+      sizeof(float) * (size_t)DftLayout(d.I, d.M, d.K, d.I == 256 ? 2 : 4).total > 227 * 1024)
+    return LBM_ERR_ARG;
   return LBM_OK;
 }
 
@@ -980,7 +1005,7 @@ template <typename R> int prime(const lbm_stepper_desc* desc, cudaStream_t st) {
   constexpr int JG = Cfg<R>::JG, KC = Cfg<R>::KCS;
   const int JH = d.J / 2, NRmax = d.N + 2, NP = (d.M + 1) / 2;
   const int NJG = (JH + JG - 1) / JG;
-  int nt = 2 * NJG * KC;
+  int nt = NJG * KC;
   nt = nt > 512 ? 512 : ((nt + 31) / 32) * 32;
   k_synth<R, JG, KC><<<dim3(NP, d.E, (d.K + KC - 1) / KC), nt, synth_smem<R>(NRmax, JH), st>>>(d);
   LBM_LAUNCH_CHECK();

@@ -58,6 +58,11 @@ class EnsembleStepper:
         self.symp = R(sp.pnm[self.pm, self.pn, :JH])
         self.symh = R(sp.hnm[self.pm, self.pn, :JH])
         self.tw = R(sp._tw64)
+        # longitude DFT table of the FP32 grid kernel: (cos, sin)(2 pi m i/I), i <= I/4
+        Q = I // 4
+        ang = 2.0 * np.pi * np.outer(np.arange(M), np.arange(Q + 1)) / I
+        self.dft = torch.as_tensor(np.stack([np.cos(ang), np.sin(ang)], -1),
+                                   device=dev, dtype=torch.float32).contiguous()
         coslat = sp.coslat
         gwdel = torch.as_tensor(sp.gwdel, device=dev)
         self.jfac = R(torch.stack([torch.as_tensor(sp.gw, device=dev), gwdel * coslat,
@@ -224,6 +229,7 @@ class EnsembleStepper:
         d.vdiff = ptr(self.vdm)
         d.frc3 = ptr(self.frc3)
         d.frcs = ptr(self.frcs)
+        d.dft = ptr(self.dft)
         d.err = C.cast(C.c_void_p(self.err.data_ptr()), C.POINTER(C.c_int))
         self._desc = d
         return d
