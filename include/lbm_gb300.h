@@ -31,6 +31,8 @@ extern "C" {
 #define LBM_ERR_LAUNCH 2       /* CUDA launch or runtime failure               */
 #define LBM_ERR_SINGULAR 3     /* zero pivot in a factorisation                */
 #define LBM_ERR_NONFINITE 4    /* non-finite prognostic value detected         */
+#define LBM_ERR_SCRATCH 5      /* case larger than the static scratch area of
+                                  lbm_stepper_run_noalloc                      */
 
 /* ---- precisions ------------------------------------------------------------- */
 #define LBM_F64 0
@@ -72,7 +74,8 @@ int lbm_gravity_wave_matrices(int nmax, int kmax, double dt, const double* lap,
 /* Batched inverse by Gauss-Jordan elimination with partial pivoting, FP64
  * (xp.linalg.inv at integrator.py:161 and numpy inv at integrator.py:226).
  * a, ainv: [batch][n][n]; info[batch] = 0, or 1 + the column of a zero pivot
- * (then LBM_ERR_SINGULAR is reported by lbm_check_info). n <= 64. */
+ * (the caller reads info after the stream completes; a nonzero entry means
+ * that matrix is singular). n <= 64. */
 int lbm_batched_inverse(int batch, int n, const double* a, double* ainv,
                         int* info, void* stream);
 
@@ -259,6 +262,46 @@ int lbm_graph_capture(const lbm_stepper_desc* d, const lbm_step_ctl* ctl,
                       int nsteps, void* stream, lbm_graph** out);
 int lbm_graph_launch(lbm_graph* g, void* stream);
 int lbm_graph_destroy(lbm_graph* g);
+
+/* ---- Stepping without allocating -------------------------------------------
+ * No counterpart in the reference, whose step functions allocate their work
+ * arrays through the array backend on every call.
+ *
+ * lbm_stepper_run_noalloc is lbm_stepper_prime followed by lbm_stepper_run
+ * (same kernels, same results) for callers that cannot allocate device
+ * memory for the six intermediate buffers sf, sfs, af, afs, tend, tends: a
+ * host that embeds the dynamical core behind an FFI and hands the library
+ * only its state, operator and forcing buffers -- for instance because all of
+ * its device memory belongs to another runtime's pool, or because cudaMalloc
+ * and cudaFree synchronise the device in the middle of its time loop -- and
+ * that does not want to keep those buffers (6.2 MiB per member at T42L20 in
+ * FP32, twice that in FP64) alive between calls.
+ *
+ * The intermediates come instead from one static device array of
+ * LBM_NOALLOC_SCRATCH_BYTES, which every GPU that loads the library holds
+ * until the process exits.  The call allocates nothing: no cudaMalloc, no
+ * cudaFree, no allocating library routine.
+ *   - d: as for lbm_stepper_run; its sf, sfs, af, afs, tend and tends are
+ *     ignored (may be NULL).  Every other pointer is the caller's, and the
+ *     state (sa3, sas, sb3, psa, psb, err) is updated in place.
+ *   - The call needs E * M * J * (13 K + 7) + E * NS * (4 K + 2) complex
+ *     values (each buffer rounded up to 256 bytes); a case larger than
+ *     LBM_NOALLOC_SCRATCH_BYTES is rejected with LBM_ERR_SCRATCH before
+ *     anything is launched (at most 5 members at T42L20 in FP32, 2 in FP64;
+ *     20 and 10 at T21L20).
+ *   - Each call first clears the part of the area it uses (cudaMemsetAsync
+ *     on `stream`) and synthesises the current level into it, so nothing
+ *     carries over from an earlier call: the state in d is all there is.
+ *   - Set-up: the first call on a device looks up the array's address with
+ *     cudaGetSymbolAddress, with that device current, and keeps it.  Make the
+ *     first call on each device before any stream capture begins.
+ *   - The area is shared by every call on a device: two calls whose work
+ *     overlaps on the GPU (different streams, or different host threads with
+ *     no ordering between them) race on it and give wrong results.  Order
+ *     them on one stream or with events. */
+#define LBM_NOALLOC_SCRATCH_BYTES (32u << 20) /* 32 MiB per device */
+int lbm_stepper_run_noalloc(const lbm_stepper_desc* d, const lbm_step_ctl* ctl,
+                            int nsteps, void* stream);
 
 #ifdef __cplusplus
 }

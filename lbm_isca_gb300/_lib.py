@@ -12,6 +12,8 @@ import os
 from .build import LIBPATH
 
 LBM_OK, LBM_ERR_ARG, LBM_ERR_LAUNCH, LBM_ERR_SINGULAR, LBM_ERR_NONFINITE = 0, 1, 2, 3, 4
+LBM_ERR_SCRATCH = 5
+LBM_NOALLOC_SCRATCH_BYTES = 32 << 20
 LBM_F64, LBM_F32 = 0, 1
 _STATUS = {LBM_ERR_ARG: "bad argument or unsupported size",
            LBM_ERR_LAUNCH: "CUDA launch/runtime failure",
@@ -86,6 +88,7 @@ _SIGS = {
                                 C.POINTER(VP)]),
     "lbm_graph_launch": (I32, [VP, VP]),
     "lbm_graph_destroy": (I32, [VP]),
+    "lbm_stepper_run_noalloc": (I32, [C.POINTER(StepperDesc), C.POINTER(StepCtl), I32, VP]),
 }
 
 _LIB = None

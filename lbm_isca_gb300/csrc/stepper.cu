@@ -25,6 +25,8 @@
 // no second pass over the levels.
 #include "lbm_common.cuh"
 #include "lbm_fft.cuh"
+#include <cmath>
+#include <mutex>
 #include <new>
 #include <type_traits>
 
@@ -1034,6 +1036,65 @@ template <typename R> int flush(const lbm_stepper_desc* desc, int ps_mode, cudaS
   return LBM_OK;
 }
 
+// ---- stepping from a static scratch area ------------------------------------
+// lbm_stepper_run_noalloc takes the six intermediate buffers of a step (sf,
+// sfs, af, afs, tend, tends) from this file-scope array instead of caller
+// memory.  It is sized once, at LBM_NOALLOC_SCRATCH_BYTES, and every GPU that
+// loads the library holds it until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[LBM_NOALLOC_SCRATCH_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_base[NOALLOC_MAX_DEVICES];
+
+// Byte offsets of sf, sfs, af, afs, tend, tends in the scratch area, each
+// rounded up to 256 bytes.  `need` is the total, computed in double so that
+// an absurd size cannot wrap around before it is compared with the maximum.
+static void noalloc_layout(const lbm_stepper_desc& d, size_t off[6], double* need) {
+  const double c = 2.0 * (d.prec == LBM_F64 ? sizeof(double) : sizeof(float));
+  const double E = d.nmem, M = d.nmax + 1.0, J = d.nlat, K = d.kmax;
+  const double NS = M * (M + 1.0) / 2.0;
+  const double n[6] = {E * M * J * K * 6, E * M * J * 5, E * M * J * K * 7,
+                       E * M * J * 2,     E * 4 * NS * K, E * 2 * NS};
+  double t = 0.0;
+  for (int i = 0; i < 6; ++i) {
+    off[i] = (size_t)t;
+    t += 256.0 * std::ceil(n[i] * c / 256.0);
+  }
+  *need = t;
+}
+
+// Device address of the scratch area on the current device.  The first call
+// on a device looks it up with cudaGetSymbolAddress (with that device
+// current) and keeps it; later calls reuse it.
+static int noalloc_base(void** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+    return LBM_ERR_LAUNCH;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_base[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return LBM_ERR_LAUNCH;
+    g_noalloc_base[dev] = p;
+  }
+  *out = g_noalloc_base[dev];
+  return LBM_OK;
+}
+
+template <typename R> int run_noalloc(const lbm_stepper_desc& w, const lbm_step_ctl* ctl,
+                                      int nsteps, size_t clear, cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(st, &cs);
+  if (cs == cudaStreamCaptureStatusNone) {
+    const int rc = prepare_attrs<R>(&w);
+    if (rc) return rc;
+  }
+  if (cudaMemsetAsync(w.sf, 0, clear, st) != cudaSuccess) return LBM_ERR_LAUNCH;
+  const int rc = prime<R>(&w, st);
+  if (rc) return rc;
+  return run_steps<R>(&w, ctl, nsteps, st);
+}
+
 }  // namespace lbm
 
 using namespace lbm;
@@ -1133,6 +1194,35 @@ int lbm_graph_destroy(lbm_graph* g) {
   cudaGraphDestroy(g->graph);
   delete g;
   return LBM_OK;
+}
+
+int lbm_stepper_run_noalloc(const lbm_stepper_desc* d, const lbm_step_ctl* ctl, int nsteps,
+                            void* stream) {
+  if (!d || !ctl || nsteps < 0 || (d->prec != LBM_F64 && d->prec != LBM_F32)) return LBM_ERR_ARG;
+  if (d->nmem < 1 || d->nlat < 2 || d->nmax < 1 || d->kmax < 1) return LBM_ERR_ARG;
+  size_t off[6];
+  double need = 0.0;
+  noalloc_layout(*d, off, &need);
+  if (need > (double)LBM_NOALLOC_SCRATCH_BYTES) return LBM_ERR_SCRATCH;
+  for (int s = 0; s < nsteps; ++s)
+    if (ctl[s].set < 0 || ctl[s].set >= d->nsets || ctl[s].ps_mode < 0 || ctl[s].ps_mode > 2 ||
+        ctl[s].ra_mode < 0 || ctl[s].ra_mode > 1)
+      return LBM_ERR_ARG;
+  void* base = nullptr;
+  const int rc = noalloc_base(&base);
+  if (rc) return rc;
+  unsigned char* b = static_cast<unsigned char*>(base);
+  lbm_stepper_desc w = *d;
+  w.sf = b + off[0];
+  w.sfs = b + off[1];
+  w.af = b + off[2];
+  w.afs = b + off[3];
+  w.tend = b + off[4];
+  w.tends = b + off[5];
+  const size_t clear = (size_t)need;
+  cudaStream_t st = (cudaStream_t)stream;
+  return d->prec == LBM_F64 ? run_noalloc<double>(w, ctl, nsteps, clear, st)
+                            : run_noalloc<float>(w, ctl, nsteps, clear, st);
 }
 
 }  // extern "C"

@@ -41,3 +41,17 @@ def test_bad_arguments_are_rejected_without_a_device():
                                  None) == _lib.LBM_ERR_ARG
     assert L.lbm_stepper_run(None, None, 1, None) == _lib.LBM_ERR_ARG
     assert L.lbm_batched_inverse(1, 65, None, None, None, None) == _lib.LBM_ERR_ARG
+
+
+def test_noalloc_stepper_rejects_oversized_cases_without_a_device():
+    """The static-scratch stepper checks its size before any CUDA call."""
+    import ctypes as C
+    from lbm_isca_gb300 import _lib
+    L = _lib.lib()
+    d = _lib.StepperDesc()
+    d.prec, d.nmem, d.nlat, d.nlon, d.nmax, d.kmax, d.nsets = _lib.LBM_F32, 6, 64, 128, 42, 20, 1
+    ctl = (_lib.StepCtl * 1)()
+    assert L.lbm_stepper_run_noalloc(C.byref(d), ctl, 1, None) == _lib.LBM_ERR_SCRATCH
+    d.nmem = 0
+    assert L.lbm_stepper_run_noalloc(C.byref(d), ctl, 1, None) == _lib.LBM_ERR_ARG
+    assert L.lbm_stepper_run_noalloc(None, ctl, 1, None) == _lib.LBM_ERR_ARG
