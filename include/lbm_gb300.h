@@ -188,12 +188,19 @@ int lbm_implicit_step(int prec, const lbm_implicit_args* a, void* stream);
  *   symp, symh [NS][J/2]       P and H at the northern latitudes, packed rows
  *   tw [I] cplx; jfac [4][J]: gw, gwdel*coslat, 1/(a coslat), coslat
  *   vert [16][K+1]: see LBM_VERT_* below
- *   b3 [10][J][K][I]: ub vb tb qb tvb absvor divb x5b tdev tvdev
+ *   b3 [14][J][K][I]: ub vb tb qb tvb absvor divb x5b tdev tvdev, then the
+ *                   half vertical differences 0.5 (f[k+1] - f[k]) of ub vb tb
+ *                   qb (0 at the top level)
  *   bsd [J][K+1][I] basic sigma-dot; b2 [5][J][I]: pixb piyb psbar
  *                   sum_k dsig ub, sum_k dsig vb
  *   ops: lap, invlap, nn1a [M]; kv kd ktt kq [M][K]; ww tmtx [K][K];
  *        minv [nsets][M][K][K] (stored transposed: [n][l][k]);
- *        vdiff [nsets][4][K][K] (transposed) with vd_on[4] flags
+ *        vdiff [nsets][4][K][K]: implicit vertical-diffusion operator minus
+ *        the identity, transposed, with vd_on[4] flags.  ww and tmtx are not
+ *        read (may be NULL): the kernels apply both through their level-scan
+ *        forms from vert, (WW x)_k = RALPHA_k x_k + sum_{l<k} RDLOG3_l x_l and
+ *        (tmtx D)_k = KTREF_k (ALPHA_k D_k + W3_k sum_{l>k} DSIG_l D_l), the
+ *        structure vertical.py gives them
  *   dft [M][I/4+1] (cos, sin)(2 pi m i / I): longitude DFT table of the FP32
  *        grid kernel (may be NULL in FP64 mode)
  *   frc3 [Ef][4][NS][K], frcs [Ef][NS]: spectral forcing (NULL = none),

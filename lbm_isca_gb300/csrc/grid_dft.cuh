@@ -28,6 +28,26 @@
 
 namespace lbm {
 
+// Vertical advection of dynamics.py's _vert_advect written in differences,
+//   (s1 (f[k+1] - f[k]) / 2 + s0 (f[k] - f[k-1]) / 2) / dsig_k
+// (at the bottom / top the missing half becomes +s0 f[k] / -s1 f[k]), which
+// equals the flux form (F[k+1/2] - F[k-1/2] - f[k] (s1 - s0)) / dsig_k with
+// F = s (f[k] + f[k+-1]) / 2 without cancelling the f[k] (s1 - s0) part.
+// vadv_p: perturbation field; vadv_b: basic state with its half differences
+// hm = (f[k] - f[k-1]) / 2, hp = (f[k+1] - f[k]) / 2 precomputed in FP64.
+LBM_D float vadv_p(float fm, float f0, float fp, float s0, float s1, bool lo, bool hi,
+                   float dsk) {
+  const float up = hi ? 0.5f * s1 * (fp - f0) : -s1 * f0;
+  const float dn = lo ? 0.5f * s0 * (f0 - fm) : s0 * f0;
+  return (up + dn) / dsk;
+}
+LBM_D float vadv_b(float f0, float hm, float hp, float s0, float s1, bool lo, bool hi,
+                   float dsk) {
+  const float up = hi ? s1 * hp : -s1 * f0;
+  const float dn = lo ? s0 * hm : s0 * f0;
+  return (up + dn) / dsk;
+}
+
 template <int I> struct DftGrid {
   static constexpr int Q = I / 4;
   static constexpr int NT = 256;
@@ -51,7 +71,7 @@ struct DftLayout {
     gout = o; o = al4(o + KB * 9 * I);
     fw = o; o = al4(o + KB * 9 * (Q + 1) * 4);
     pre = o; o = al4(o + KB * 5 * I);
-    pst = o; o = al4(o + 3 * I);
+    pst = o; o = al4(o + 5 * I);
     sg = o; o = al4(o + 8 * I);
     vert = o; o = al4(o + LBM_VERT_COUNT * (K + 1));
     total = o;
@@ -239,13 +259,13 @@ __global__ void __launch_bounds__(DftGrid<I>::NT) k_grid_dft(SD<float> d, const 
   float* gout = sm + L.gout;          // [KB][9][I]
   float4* fw = reinterpret_cast<float4*>(sm + L.fw);   // [KB*9][Q+1]
   float* pre = sm + L.pre;            // [KB][5][I]
-  float* pst = sm + L.pst;            // [3][I]
+  float* pst = sm + L.pst;            // [5][I]
   float* sg = sm + L.sg;              // [8][I]
   float* vert = sm + L.vert;          // [VERT][K+1]
 
   for (int x = tid; x < M * (Q + 1); x += NT) tab[x] = dft[x];
   for (int x = tid; x < LBM_VERT_COUNT * (K + 1); x += NT) vert[x] = d.vert[x];
-  for (int x = tid; x < 3 * I; x += NT) pst[x] = 0.f;
+  for (int x = tid; x < 5 * I; x += NT) pst[x] = 0.f;
   auto V = [&](int row, int k) { return vert[row * (K + 1) + k]; };
   const float gw = d.jfac[JF_GW * J + j], gwdc = d.jfac[JF_GWDELC * J + j];
   const float rcos = d.jfac[JF_RCOS * J + j];
@@ -307,8 +327,11 @@ __global__ void __launch_bounds__(DftGrid<I>::NT) k_grid_dft(SD<float> d, const 
     const float sx = pixb * uh + piyb * vh + pix * usum + piy * vsum;
     sg[3 * I + c] = pixb;                        // (slots 3, 4 reused: basic grad ln ps)
     sg[4 * I + c] = piyb;
+    sg[5 * I + c] = sx;                          // sum_k dsig v.grad(pi)
     sg[6 * I + c] = dh + sx;                     // S_tot
     sg[7 * I + c] = dh;
+    // sigma-dot at the lowest interface, (sigm_0 - 1) S_tot
+    pst[c] = (V(LBM_VERT_SIGM, 0) - 1.f) * (dh + sx);
     gout[0 * I + c] = -sx;                       // gt_pi = -sum dsig v.grad(pi)
     const size_t gp = (size_t)e * J * I + g2;
     const float pscur = psbar * expm1f(pi);
@@ -366,31 +389,38 @@ __global__ void __launch_bounds__(DftGrid<I>::NT) k_grid_dft(SD<float> d, const 
       const float tt = RG(k, SF_T)[c], qq = RG(k, SF_Q)[c];
       const float pa = uu * pixb + B3(B_U, k, c) * pix + vv * piyb + B3(B_V, k, c) * piy;
       float* pr = pre + (l * 5) * I;
-      pr[0 * I + c] = (dd + pa) * V(LBM_VERT_DSIG, k);
+      pr[0 * I + c] = (dd + pa - sg[6 * I + c]) * V(LBM_VERT_DSIG, k);
       pr[1 * I + c] = dd * V(LBM_VERT_DSIG, k);
       pr[2 * I + c] = eps * (tt * B3(B_Q, k, c) + B3(B_T, k, c) * qq);   // Tv' - T'
       pr[3 * I + c] = pa;
     }
     __syncthreads();
-    // per-column scan over the batch's levels
+    // per-column scan over the batch's levels.  sigma-dot runs as the sum of
+    // dsig (D + v.grad(pi) - S_tot) (no total-minus-prefix cancellation); the
+    // suffix sums of dsig D and of dsig v.grad(pi) are kept apart so that the
+    // temperature equation can cancel its reference-temperature part exactly
     for (int c = tid; c < I; c += NT) {
-      const float stot = sg[6 * I + c], dh = sg[7 * I + c];
-      float pref = pst[c], prefd = pst[I + c], pref3 = pst[2 * I + c];
+      const float dh = sg[7 * I + c], ptot = sg[5 * I + c];
+      float sdot = pst[c], prefd = pst[I + c], pref3 = pst[2 * I + c], prefp = pst[3 * I + c];
+      pst[4 * I + c] = sdot;                                       // lower interface of lo
       for (int l = 0; l < kb; ++l) {
         const int k = k0 + l;
         float* pr = pre + (l * 5) * I;
         const float cc = pr[0 * I + c], cd = pr[1 * I + c], x = pr[2 * I + c];
+        const float pa = pr[3 * I + c];
         pr[4 * I + c] = pref3 + V(LBM_VERT_RALPHA, k) * x;        // (WW (Tv'-T'))_k
-        pr[0 * I + c] = stot - pref;                               // S[k]
-        pref += cc;
-        pr[1 * I + c] = stot - pref;                               // S[k+1]
+        sdot += cc;
+        pr[0 * I + c] = sdot;                                      // sigma-dot at k+1/2
         prefd += cd;
         pr[2 * I + c] = dh - prefd;                                // sum_{l>k} dsig div
+        prefp += V(LBM_VERT_DSIG, k) * pa;
+        pr[1 * I + c] = ptot - prefp;                              // sum_{l>k} dsig v.grad(pi)
         pref3 += V(LBM_VERT_RDLOG3, k) * x;
       }
-      pst[c] = pref;
+      pst[c] = sdot;
       pst[I + c] = prefd;
       pst[2 * I + c] = pref3;
+      pst[3 * I + c] = prefp;
     }
     __syncthreads();
     // pointwise algebra, (level, column) per item
@@ -399,27 +429,29 @@ __global__ void __launch_bounds__(DftGrid<I>::NT) k_grid_dft(SD<float> d, const 
       const bool hasm = k >= 1, hasp = k + 1 <= K - 1;
       // basic state at k (and k-1, k+1): all global loads issued first
       const float* bk = b3j + (size_t)k * I + c;
-      const int om = hasm ? -I : 0, op = hasp ? I : 0;
+      const int om = hasm ? -I : 0;
       const float ub = __ldg(bk + B_U * b3f), vb = __ldg(bk + B_V * b3f);
       const float tb = __ldg(bk + B_T * b3f), qb = __ldg(bk + B_Q * b3f);
       const float tvb = __ldg(bk + B_TV * b3f), absv = __ldg(bk + B_ABSVOR * b3f);
       const float divb = __ldg(bk + B_DIV * b3f), x5b = __ldg(bk + B_X5 * b3f);
       const float tdev = __ldg(bk + B_TDEV * b3f), tvdev = __ldg(bk + B_TVDEV * b3f);
-      const float ubm = __ldg(bk + B_U * b3f + om), ubp = __ldg(bk + B_U * b3f + op);
-      const float vbm = __ldg(bk + B_V * b3f + om), vbp = __ldg(bk + B_V * b3f + op);
-      const float tbm = __ldg(bk + B_T * b3f + om), tbp = __ldg(bk + B_T * b3f + op);
-      const float qbm = __ldg(bk + B_Q * b3f + om), qbp = __ldg(bk + B_Q * b3f + op);
+      // half vertical differences 0.5 (f[k+1] - f[k]) of ub, vb, tb, qb at k-1 and k
+      const float hum = __ldg(bk + B_HDU * b3f + om), hup = __ldg(bk + B_HDU * b3f);
+      const float hvm = __ldg(bk + B_HDV * b3f + om), hvp = __ldg(bk + B_HDV * b3f);
+      const float htm = __ldg(bk + B_HDT * b3f + om), htp = __ldg(bk + B_HDT * b3f);
+      const float hqm = __ldg(bk + B_HDQ * b3f + om), hqp = __ldg(bk + B_HDQ * b3f);
       const float* bsdk = d.bsd + ((size_t)j * (K + 1) + k) * I + c;
       const float sb0 = __ldg(bsdk), sb1 = __ldg(bsdk + I);
       const float pix = sg[1 * I + c], piy = sg[2 * I + c];
-      const float pixb = sg[3 * I + c], piyb = sg[4 * I + c], stot = sg[6 * I + c];
+      const float pixb = sg[3 * I + c], piyb = sg[4 * I + c];
       const float* pr = pre + (l * 5) * I;
-      const float S0 = pr[0 * I + c], S1 = pr[1 * I + c], sdv = pr[2 * I + c];
+      const float sdv = pr[2 * I + c], spv = pr[1 * I + c];
       const float padv = pr[3 * I + c], phiv = pr[4 * I + c];
       const float* vk = vert + k;              // per-level constants at row * (K+1)
       const int VS = K + 1;
-      const float sd0 = hasm ? vk[LBM_VERT_SIGM * VS] * stot - S0 : 0.f;
-      const float sd1 = hasp ? vk[LBM_VERT_SIGM * VS + 1] * stot - S1 : 0.f;
+      // sigma-dot at the lower (k-1/2) and upper (k+1/2) interfaces
+      const float sd0 = hasm ? (l > 0 ? pre[((l - 1) * 5) * I + c] : pst[4 * I + c]) : 0.f;
+      const float sd1 = hasp ? pr[0 * I + c] : 0.f;
       const float dsk = vk[LBM_VERT_DSIG * VS];
       const float* r0 = ring + ((k % RS) * SF_N) * I + c;
       const float* rm = ring + (((hasm ? k - 1 : k) % RS) * SF_N) * I + c;
@@ -427,25 +459,26 @@ __global__ void __launch_bounds__(DftGrid<I>::NT) k_grid_dft(SD<float> d, const 
       const float u = r0[SF_U * I], v = r0[SF_V * I], vo = r0[SF_VOR * I];
       const float dv = r0[SF_DIV * I], tt = r0[SF_T * I], q = r0[SF_Q * I];
       const float tv = tt + eps * (tt * qb + tb * q);
-      const float x5p = vk[LBM_VERT_ALPHA * VS] * dv + vk[LBM_VERT_WP * VS] * padv +
-                        vk[LBM_VERT_W3 * VS] * S1;
-      const float adiab = -kappa * (tv * x5b + tvb * x5p);
+      const float al = vk[LBM_VERT_ALPHA * VS], w3 = vk[LBM_VERT_W3 * VS];
+      // adiabatic term plus the reference-temperature matrix, with Tref
+      // cancelled algebraically: -kappa (Tv' x5b + Tvb x5') + kappa Tref
+      // (alpha D + w3 sum_{l>k} dsig D)
+      const float adtm = -kappa * (tv * x5b + tvdev * (al * dv + w3 * sdv) +
+                                   tvb * (vk[LBM_VERT_WP * VS] * padv + w3 * spv));
       const float hadv = tt * divb + tdev * dv;
-      const float vadvT = vadv(rm[SF_T * I], tt, rp[SF_T * I], sb0, sb1, hasm, hasp, dsk) +
-                          vadv(tbm, tb, tbp, sd0, sd1, hasm, hasp, dsk);
-      const float tm = vk[LBM_VERT_KTREF * VS] *
-                       (vk[LBM_VERT_ALPHA * VS] * dv + vk[LBM_VERT_W3 * VS] * sdv);
+      const float vadvT = vadv_p(rm[SF_T * I], tt, rp[SF_T * I], sb0, sb1, hasm, hasp, dsk) +
+                          vadv_b(tb, htm, htp, sd0, sd1, hasm, hasp, dsk);
       float* go = gout + (l * NG) * I + c;
       // field order per level: 0 gt 1 xu 2 g 3 yu | 4 fu 5 fv 6 ke 7 xv | 8 yv
-      go[0 * I] = adiab + hadv + vadvT + tm;
+      go[0 * I] = adtm + hadv + vadvT;
       go[1 * I] = u * tdev + ub * tt;
       const float rcpg = vk[LBM_VERT_RCPG * VS];
       float fu = v * absv + vb * vo - rcpg * (tv * pixb + tvdev * pix);
       float fv = -u * absv - ub * vo - rcpg * (tv * piyb + tvdev * piy);
-      fu += vadv(rm[SF_U * I], u, rp[SF_U * I], sb0, sb1, hasm, hasp, dsk) +
-            vadv(ubm, ub, ubp, sd0, sd1, hasm, hasp, dsk);
-      fv += vadv(rm[SF_V * I], v, rp[SF_V * I], sb0, sb1, hasm, hasp, dsk) +
-            vadv(vbm, vb, vbp, sd0, sd1, hasm, hasp, dsk);
+      fu += vadv_p(rm[SF_U * I], u, rp[SF_U * I], sb0, sb1, hasm, hasp, dsk) +
+            vadv_b(ub, hum, hup, sd0, sd1, hasm, hasp, dsk);
+      fv += vadv_p(rm[SF_V * I], v, rp[SF_V * I], sb0, sb1, hasm, hasp, dsk) +
+            vadv_b(vb, hvm, hvp, sd0, sd1, hasm, hasp, dsk);
       go[4 * I] = fu;
       go[5 * I] = fv;
       float ke = phiv + u * ub + v * vb;
@@ -453,8 +486,8 @@ __global__ void __launch_bounds__(DftGrid<I>::NT) k_grid_dft(SD<float> d, const 
       go[6 * I] = ke;
       go[7 * I] = v * tdev + vb * tt;
       go[2 * I] = q * divb + qb * dv +
-                  vadv(rm[SF_Q * I], q, rp[SF_Q * I], sb0, sb1, hasm, hasp, dsk) +
-                  vadv(qbm, qb, qbp, sd0, sd1, hasm, hasp, dsk);
+                  vadv_p(rm[SF_Q * I], q, rp[SF_Q * I], sb0, sb1, hasm, hasp, dsk) +
+                  vadv_b(qb, hqm, hqp, sd0, sd1, hasm, hasp, dsk);
       go[3 * I] = u * qb + ub * q;
       go[8 * I] = v * qb + vb * q;
     }

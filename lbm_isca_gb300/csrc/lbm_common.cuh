@@ -32,6 +32,54 @@ template <typename R> LBM_HD void cfma(C2<R>& acc, R t, C2<R> v) {
   acc.y = fma(t, v.y, acc.y);
 }
 
+// Extended precision for sums that cancel: an unevaluated float pair hi + lo
+// built from error-free transformations (Knuth's TwoSum, the FMA form of
+// Dekker's TwoProduct) in FP32 mode; plain double in FP64 mode, where the
+// working precision already suffices.
+template <typename R> struct XF { R hi, lo; };
+template <typename R> LBM_HD XF<R> xf(R a) { return {a, R(0)}; }
+template <typename R> LBM_HD XF<R> xf_norm(R s, R e) {   // |s| >= |e|
+  const R h = s + e;
+  return {h, e - (h - s)};
+}
+template <typename R> LBM_HD XF<R> xf_add(XF<R> a, XF<R> b) {
+  if constexpr (sizeof(R) == 8) {
+    return {a.hi + b.hi, R(0)};
+  } else {
+    const R s = a.hi + b.hi, bb = s - a.hi;
+    const R e = (a.hi - (s - bb)) + (b.hi - bb);
+    return xf_norm(s, e + (a.lo + b.lo));
+  }
+}
+template <typename R> LBM_HD XF<R> xf_prod(R a, R b) {   // a b without rounding
+  if constexpr (sizeof(R) == 8) {
+    return {a * b, R(0)};
+  } else {
+    const R p = a * b;
+    return {p, fma(a, b, -p)};
+  }
+}
+template <typename R> LBM_HD XF<R> xf_mul(XF<R> a, R b) {
+  if constexpr (sizeof(R) == 8) {
+    return {a.hi * b, R(0)};
+  } else {
+    const R p = a.hi * b;
+    return xf_norm(p, fma(a.hi, b, -p) + a.lo * b);
+  }
+}
+template <typename R> LBM_HD XF<R> xf_neg(XF<R> a) { return {-a.hi, -a.lo}; }
+template <typename R> LBM_HD R xf_val(XF<R> a) { return a.hi + a.lo; }
+// complex pairs of XF
+template <typename R> struct CX { XF<R> x, y; };
+template <typename R> LBM_HD CX<R> cx(C2<R> a) { return {xf(a.x), xf(a.y)}; }
+template <typename R> LBM_HD CX<R> cx_add(CX<R> a, CX<R> b) {
+  return {xf_add(a.x, b.x), xf_add(a.y, b.y)};
+}
+template <typename R> LBM_HD CX<R> cx_prod(R s, C2<R> v) { return {xf_prod(s, v.x), xf_prod(s, v.y)}; }
+template <typename R> LBM_HD CX<R> cx_mul(CX<R> a, R s) { return {xf_mul(a.x, s), xf_mul(a.y, s)}; }
+template <typename R> LBM_HD CX<R> cx_neg(CX<R> a) { return {xf_neg(a.x), xf_neg(a.y)}; }
+template <typename R> LBM_HD C2<R> cx_val(CX<R> a) { return cmk(xf_val(a.x), xf_val(a.y)); }
+
 template <typename R> struct Prec;
 template <> struct Prec<float> { static constexpr int id = LBM_F32; };
 template <> struct Prec<double> { static constexpr int id = LBM_F64; };

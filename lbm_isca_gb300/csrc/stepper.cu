@@ -74,7 +74,8 @@ template <typename R> SD<R> make_sd(const lbm_stepper_desc& d) {
 }
 
 // basic-state 3-D field indices in b3 [10][J][K][I]
-enum { B_U = 0, B_V, B_T, B_Q, B_TV, B_ABSVOR, B_DIV, B_X5, B_TDEV, B_TVDEV };
+enum { B_U = 0, B_V, B_T, B_Q, B_TV, B_ABSVOR, B_DIV, B_X5, B_TDEV, B_TVDEV,
+       B_HDU, B_HDV, B_HDT, B_HDQ, B_N };
 // b2 [5][J][I]
 enum { B2_PIX = 0, B2_PIY, B2_PSBAR, B2_USUM, B2_VSUM };
 // jfac [4][J]
@@ -491,6 +492,18 @@ __global__ void k_anal(SD<R> d) {
 // =============================================================================
 constexpr int IM_THREADS = 256;
 
+// The semi-implicit update in the order of integrator.py:264-315.  Three
+// places subtract nearly equal quantities, and the FP32 mode carries them in
+// float-float (XF) so that the difference keeps FP32 relative precision:
+// the divergence right-hand side (explicit tendency against the Laplacian of
+// the geopotential), the temperature update (heating against the
+// reference-temperature matrix on the mean divergence) and the pi update
+// (against the column-integrated divergence).  WW and tmtx enter through
+// their level-scan forms
+//   (WW x)_k   = R alpha_k x_k + sum_{l<k} R dlog3_l x_l,
+//   (tmtx D)_k = kappa Tref_k (alpha_k D_k + w3_k sum_{l>k} dsig_l D_l),
+// each level summing its own prefix / suffix.  Damping factors 1 / (1 + c)
+// are applied as x - x c / (1 + c) so that a small c keeps its precision.
 template <typename R>
 __global__ void __launch_bounds__(IM_THREADS) k_implicit(SD<R> d, R dt, int set, int ra_mode) {
   const int p = blockIdx.x, e = blockIdx.y;
@@ -501,25 +514,30 @@ __global__ void __launch_bounds__(IM_THREADS) k_implicit(SD<R> d, R dt, int set,
   const int CC = IM_THREADS / K;               // coefficients per chunk
   extern __shared__ unsigned char smraw[];
   R* mi = reinterpret_cast<R*>(smraw);          // [2][K][K] minv^T (l, k)
-  R* wwT = mi + 2 * K * K;                      // [K][K] (l, k)
-  R* tmT = wwT + K * K;                         // [K][K] (l, k)
-  R* vdT = tmT + K * K;                         // [4][K][K] (l, k)
-  C2<R>* bA = reinterpret_cast<C2<R>*>(vdT + 4 * K * K);   // [CC][K]
-  C2<R>* bB = bA + CC * K;
-  C2<R>* bC = bB + CC * K;
+  R* vdT = mi + 2 * K * K;                      // [4][K][K] (vdiff - I)^T (l, k)
+  R* vs = vdT + 4 * K * K;                      // [6][K] RALPHA RDLOG3 GG DSIG ALPHA W3
+  R* ktr = vs + 6 * K;                          // [K] KTREF
+  C2<R>* bA = reinterpret_cast<C2<R>*>(ktr + K + (K & 1));  // [CC][K]
+  C2<R>* bB = bA + CC * K;                                   // [CC][K]
   const int tid = threadIdx.x;
   const R* mset = d.minv + (size_t)set * d.M * K * K;
   for (int idx = tid; idx < K * K; idx += IM_THREADS) {
     mi[idx] = mset[(size_t)n1 * K * K + idx];
     mi[K * K + idx] = mset[(size_t)n2 * K * K + idx];
-    const int l = idx / K, k = idx % K;
-    wwT[idx] = d.ww[k * K + l];
-    tmT[idx] = d.tmtx[k * K + l];
   }
   for (int f = 0; f < 4; ++f)
     if (d.vd_on[f])
       for (int idx = tid; idx < K * K; idx += IM_THREADS)
         vdT[f * K * K + idx] = d.vdiff[((size_t)set * 4 + f) * K * K + idx];
+  for (int idx = tid; idx < K; idx += IM_THREADS) {
+    vs[0 * K + idx] = vrow(d, LBM_VERT_RALPHA, idx);
+    vs[1 * K + idx] = vrow(d, LBM_VERT_RDLOG3, idx);
+    vs[2 * K + idx] = vrow(d, LBM_VERT_GG, idx);
+    vs[3 * K + idx] = vrow(d, LBM_VERT_DSIG, idx);
+    vs[4 * K + idx] = vrow(d, LBM_VERT_ALPHA, idx);
+    vs[5 * K + idx] = vrow(d, LBM_VERT_W3, idx);
+    ktr[idx] = vrow(d, LBM_VERT_KTREF, idx);
+  }
   __syncthreads();
   const R dt2 = R(2) * dt, gam = d.robert;
   const C2<R> z = cmk<R>(0, 0);
@@ -557,46 +575,54 @@ __global__ void __launch_bounds__(IM_THREADS) k_implicit(SD<R> d, R dt, int set,
       ktt = d.ktt[n * K + k]; kd = d.kd[n * K + k]; kv = d.kv[n * K + k]; kq = d.kq[n * K + k];
       lap = d.lap[n];
     }
-    const R ft = R(1) + dt2 * ktt;
     C2<R>* A = bA + c * K;
     C2<R>* B = bB + c * K;
-    C2<R>* Cb = bC + c * K;
+    const R bt = dt2 * ktt;                      // 2 dt ktt; ft = 1 + bt
     __syncthreads();
-    if (act) A[k] = bT * (R(1) + dt * ktt) + wT * dt;     // wdx (integrator.py:287)
+    // wdx = T(t-dt) (1 + dt ktt) + dt wT  (integrator.py:287)
+    if (act) A[k] = bT + (bT * ktt + wT) * dt;
     __syncthreads();
-    C2<R> rhs = z;
     if (act) {
-      C2<R> wdphix = z;
-      for (int l = 0; l < K; ++l) cfma(wdphix, wwT[l * K + k], A[l]);
+      CX<R> phi = cx_prod(vs[0 * K + k], A[k]);            // WW wdx
+      for (int l = 0; l < k; ++l) phi = cx_add(phi, cx_prod(vs[1 * K + l], A[l]));
       const C2<R> wdpix = pp + wpi * dt;
-      const C2<R> wdphiy = wdphix + wdpix * (ft * vrow(d, LBM_VERT_GG, k));
-      rhs = bD * ((R(1) + dt * kd) * ft) + (wD * ft - wdphiy * lap) * dt;
-      B[k] = rhs;
+      const R gk = vs[2 * K + k];
+      // wdphiy = WW wdx + ft gg wdpix, ft gg taken as gg + bt gg
+      phi = cx_add(phi, cx_add(cx_prod(gk, wdpix), cx_mul(cx_prod(bt, wdpix), gk)));
+      // dt (wD ft - lap wdphiy), the two terms nearly balancing
+      const CX<R> zz = cx_add(cx_add(cx(wD), cx_prod(bt, wD)), cx_mul(phi, -lap));
+      const R ad = dt * kd;
+      B[k] = bD + (bD * (ad + bt + ad * bt) + cx_val(zz) * dt);
     }
     __syncthreads();
     C2<R> dbar = z;
     if (act) {
       const R* mm_ = mi + sel * K * K;
       for (int l = 0; l < K; ++l) cfma(dbar, mm_[l * K + k], B[l]);   // minv stored (l, k)
-      Cb[k] = dbar;
     }
+    __syncthreads();
+    if (act) A[k] = dbar;
     __syncthreads();
     C2<R> nV = z, nD = z, nT = z, nQ = z, npi = z;
     if (act) {
-      C2<R> corr = z, dsum = z;
-      for (int l = 0; l < K; ++l) {
-        cfma(corr, tmT[l * K + k], Cb[l]);
-        cfma(dsum, vrow(d, LBM_VERT_DSIG, l), Cb[l]);
+      CX<R> sfx = cx<R>(z);                                 // sum_{l>k} dsig_l dbar_l
+      for (int l = K - 1; l > k; --l) sfx = cx_add(sfx, cx_prod(vs[3 * K + l], A[l]));
+      const CX<R> corr = cx_mul(cx_add(cx_prod(vs[4 * K + k], dbar), cx_mul(sfx, vs[5 * K + k])),
+                                ktr[k]);
+      const C2<R> yT = bT + cx_val(cx_add(cx(wT), cx_neg(corr))) * dt2;
+      nT = yT - yT * (bt / (R(1) + bt));
+      if (k == 0) {
+        const CX<R> dsum = cx_add(sfx, cx_prod(vs[3 * K], dbar));
+        npi = pp + cx_val(cx_add(cx(wpi), cx_neg(dsum))) * dt2;
       }
-      const C2<R> wT2 = wT - corr;
-      const C2<R> wpi2 = wpi - dsum;
-      nV = (bV + wV * dt2) * (R(1) / (R(1) + dt2 * kv));
       nD = dbar * R(2) - bD;
-      nT = (bT + wT2 * dt2) * (R(1) / ft);
-      nQ = (bQ + wQ * dt2) * (R(1) / (R(1) + dt2 * kq));
-      npi = pp + wpi2 * dt2;
+      const R av = dt2 * kv, aq = dt2 * kq;
+      const C2<R> xV = bV + wV * dt2, xQ = bQ + wQ * dt2;
+      nV = xV - xV * (av / (R(1) + av));
+      nQ = xQ - xQ * (aq / (R(1) + aq));
     }
-    // implicit vertical diffusion (integrator.py:311-314)
+    // implicit vertical diffusion (integrator.py:311-314); vdT holds the
+    // operator minus the identity
     C2<R>* vals[4] = {&nV, &nD, &nT, &nQ};
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
@@ -605,7 +631,7 @@ __global__ void __launch_bounds__(IM_THREADS) k_implicit(SD<R> d, R dt, int set,
       if (act) A[k] = *vals[f];
       __syncthreads();
       if (act && !(f < 2 && n < 2)) {
-        C2<R> o2 = z;
+        C2<R> o2 = *vals[f];
         const R* vm = vdT + f * K * K;
         for (int l = 0; l < K; ++l) cfma(o2, vm[l * K + k], A[l]);
         *vals[f] = o2;
@@ -636,17 +662,17 @@ __global__ void __launch_bounds__(IM_THREADS) k_implicit(SD<R> d, R dt, int set,
     if (act) { A[k] = nV; B[k] = nD; }
     __syncthreads();
     if (act && k == 0) {
-      C2<R> sv = z, sdv = z;
+      CX<R> sv = cx<R>(z), sdv = cx<R>(z);
       for (int l = 0; l < K; ++l) {
-        cfma(sv, vrow(d, LBM_VERT_DSIG, l), A[l]);
-        cfma(sdv, vrow(d, LBM_VERT_DSIG, l), B[l]);
+        sv = cx_add(sv, cx_prod(vs[3 * K + l], A[l]));
+        sdv = cx_add(sdv, cx_prod(vs[3 * K + l], B[l]));
       }
       const R il = d.invlap[n];
       const size_t es = (size_t)e * 4 * NS;
       d.sas[es + 0 * NS + idx] = npi;
-      d.sas[es + 1 * NS + idx] = sv * il;     // sum dsig psi
-      d.sas[es + 2 * NS + idx] = sdv * il;    // sum dsig chi
-      d.sas[es + 3 * NS + idx] = sdv;         // sum dsig div
+      d.sas[es + 1 * NS + idx] = cx_val(cx_mul(sv, il));     // sum dsig psi
+      d.sas[es + 2 * NS + idx] = cx_val(cx_mul(sdv, il));    // sum dsig chi
+      d.sas[es + 3 * NS + idx] = cx_val(sdv);                // sum dsig div
     }
   }
 }
@@ -875,8 +901,8 @@ template <typename R> size_t synth_smem(int NR, int JH) {
   return sizeof(R) * 2 * (size_t)NR * JH + sizeof(C2<R>) * (size_t)NR * Cfg<R>::KCS * 6;
 }
 template <typename R> size_t impl_smem(int K) {
-  return sizeof(R) * (size_t)(2 + 1 + 1 + 4) * K * K +
-         sizeof(C2<R>) * 3 * (size_t)(IM_THREADS / K) * K;
+  return sizeof(R) * ((size_t)(2 + 4) * K * K + 7 * (size_t)K + (K & 1)) +
+         sizeof(C2<R>) * 2 * (size_t)(IM_THREADS / K) * K;
 }
 
 template <typename R, int I> int launch_step(const SD<R>& d, const lbm_step_ctl& c,
@@ -945,8 +971,8 @@ template <typename R> int validate(const SD<R>& d) {
   if (d.I != 64 && d.I != 128 && d.I != 256) return LBM_ERR_ARG;
   if (IM_THREADS / d.K < 1) return LBM_ERR_ARG;
   if (!d.symp || !d.symh || !d.tw || !d.jfac || !d.vert || !d.b3 || !d.bsd || !d.b2 ||
-      !d.lap || !d.invlap || !d.nn1a || !d.kv || !d.kd || !d.ktt || !d.kq || !d.ww ||
-      !d.tmtx || !d.minv || !d.sa3 || !d.sas || !d.sb3 || !d.psa || !d.psb || !d.sf ||
+      !d.lap || !d.invlap || !d.nn1a || !d.kv || !d.kd || !d.ktt || !d.kq ||
+      !d.minv || !d.sa3 || !d.sas || !d.sb3 || !d.psa || !d.psb || !d.sf ||
       !d.sfs || !d.af || !d.afs || !d.tend || !d.tends || !d.err)
     return LBM_ERR_ARG;
   for (int f = 0; f < 4; ++f)

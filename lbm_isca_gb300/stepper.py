@@ -84,8 +84,13 @@ class EnsembleStepper:
         self.vert = R(torch.as_tensor(vert))
         tref = torch.as_tensor(vh("tbar"), device=dev)
         b = bst
-        f3 = [b.u, b.v, b.t, b.q, b.tv, b.absvor, b.div, b.x5, b.t - tref, b.tv - tref]
-        self.b3 = R(torch.stack([x.permute(0, 2, 1) for x in f3]))        # [10][J][K][I]
+        def half_diff(x):          # 0.5 (x[k+1] - x[k]), 0 at the top level (FP64)
+            h = torch.zeros_like(x)
+            h[..., :-1] = 0.5 * (x[..., 1:] - x[..., :-1])
+            return h
+        f3 = [b.u, b.v, b.t, b.q, b.tv, b.absvor, b.div, b.x5, b.t - tref, b.tv - tref,
+              half_diff(b.u), half_diff(b.v), half_diff(b.t), half_diff(b.q)]
+        self.b3 = R(torch.stack([x.permute(0, 2, 1) for x in f3]))        # [14][J][K][I]
         self.bsd = R(b.sdot.permute(0, 2, 1))                             # [J][K+1][I]
         dsig = torch.as_tensor(vh("dsig"), device=dev)
         self.b2 = R(torch.stack([b.pix, b.piy, b.ps, (b.u * dsig).sum(-1),
@@ -130,7 +135,9 @@ class EnsembleStepper:
             mins.append(minv.transpose(1, 2))                    # stored (n, l, k)
             ops = self.vdiff.operators(dt)
             eye = torch.eye(K, device=self.dev, dtype=torch.float64)
-            vds.append(torch.stack([(ops[n] if ops[n] is not None else eye).T
+            # stored as (operator - identity)^T: the kernel adds the small
+            # correction to the value itself, keeping its relative precision
+            vds.append(torch.stack([((ops[n] - eye) if ops[n] is not None else 0 * eye).T
                                     for n in ("vor", "div", "t", "q")]))
         self.minv = torch.stack(mins).to(self.rd).contiguous()   # [nsets][M][K][K]
         self.vdm = torch.stack(vds).to(self.rd).contiguous()     # [nsets][4][K][K]

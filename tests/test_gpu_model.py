@@ -261,3 +261,27 @@ def test_gill_day6_matches_reference_record():
         assert abs(val - rec[key]) <= 1e-9 * max(1.0, abs(rec[key])), (key, val, rec[key])
     d = m.diagnostics()
     assert set(d) == {"psi", "chi", "u", "v", "w", "t", "z", "p"}
+
+
+def test_fp32_ensemble_within_1e5_of_fp64_at_day10():
+    """The FP32 stepper stays within 1e-5 relative L2 of the FP64 stepper (which
+    equals the oracle to 1e-10) for every prognostic field after 10 days at
+    T42L20: seeded elliptic heatings, solid-body basic state, plain damping."""
+    import torch
+    from lbm_isca_gb300 import Config
+    from lbm_isca_gb300.ensemble import EnsembleForcing, make_ensemble_model
+    sigm = configs.equal_sigma_half_levels(20)
+    bs = configs.solid_body_basic_state(128, 64, sigm)
+    heats, _ = configs.ensemble_heating(128, 64, sigm, 4, seed=1)
+    out = {}
+    for prec in ("fp64", "fp32"):
+        m, _, _ = make_ensemble_model(
+            bs, 4, Config(ndays=10.0, precision=prec, **configs.plain_damping(20)),
+            device="gb300", nlon=128, nlat=64, nmax=42, sigm=sigm)
+        m.run(mjo_forcing=EnsembleForcing(heats, device="gb300"), verbose=False)
+        a, _ = m.stepper().spectral_state()
+        out[prec] = {k: v.cpu() for k, v in a.items()}
+    for k in ("vor", "div", "t", "pi"):
+        r, f = out["fp64"][k], out["fp32"][k]
+        e = float(torch.linalg.norm(f - r) / torch.linalg.norm(r))
+        assert e <= 1e-5, (k, e)
