@@ -359,6 +359,22 @@ template <typename R> struct PairRows {
   LBM_D int n_of(int r) const { return r < L1 ? m1 + r : m2 + (r - L1); }
 };
 
+// Asynchronous global -> shared copy of 16 bytes (cp.async).
+LBM_D void cp_async_16b(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+// Asynchronous global -> shared copy of one complex value (cp.async).
+template <typename R> LBM_D void cp_async_c2(C2<R>* smem, const C2<R>* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  if constexpr (sizeof(C2<R>) == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+LBM_D void cp_async_commit_group() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+LBM_D void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
 template <typename R, int NC, int KC>
 __global__ void k_anal(SD<R> d) {
   const int p = blockIdx.x, e = blockIdx.y, kc = blockIdx.z;
@@ -369,7 +385,12 @@ __global__ void k_anal(SD<R> d) {
   extern __shared__ unsigned char smraw[];
   R* tp = reinterpret_cast<R*>(smraw);                 // [NR][JH]
   R* th = tp + pr.NR * JH;                             // [NR][JH]
-  C2<R>* xs = reinterpret_cast<C2<R>*>(th + pr.NR * JH);   // [2][AN_JC][KC][7][2]
+  // rows of AN_JC latitude pairs, two buffers, each
+  // [2 m][AN_JC][2 hemispheres][KC levels][7 fields] (an odd stride of 7
+  // complex values between lanes: no bank conflicts)
+  // (16-byte aligned)
+  C2<R>* raw = reinterpret_cast<C2<R>*>(
+      (reinterpret_cast<uintptr_t>(th + pr.NR * JH) + 15) & ~uintptr_t(15));
   const int tid = threadIdx.x, nt = blockDim.x;
   // tables for the pair's rows
   const int off1 = spec_offset(pr.m1, N), off2 = spec_offset(pr.m2, N);
@@ -392,30 +413,51 @@ __global__ void k_anal(SD<R> d) {
   const size_t jmK = (size_t)J * K;
   const C2<R>* afe = d.af + (size_t)e * M * jmK * AF_N;
   const int nm = pr.L2 ? 2 : 1;
+  const int rowlen = kn * AF_N;                 // complex values per (m, latitude) row
+  const int rowst = KC * AF_N;                  // row stride in the buffer
+  const size_t rawbuf = (size_t)2 * AN_JC * 2 * rowst;
+  // 16-byte copies when every row starts and ends on a 16-byte boundary
+  constexpr int PER = 16 / (int)sizeof(C2<R>);
+  const bool wide = ((K * AF_N) % PER == 0) && ((k0 * AF_N) % PER == 0) &&
+                    (rowlen % PER == 0) && (rowst % PER == 0);
+  auto prefetch = [&](int jh0, int b) {
+    const int jc = min(AN_JC, JH - jh0);
+    C2<R>* rb = raw + b * rawbuf;
+    const int step = wide ? PER : 1;
+    const int nchunk = rowlen / step;
+    for (int x = tid; x < nm * jc * 2 * nchunk; x += nt) {
+      const int c = (x % nchunk) * step, w = x / nchunk;
+      const int hemi = w & 1, jj = (w >> 1) % jc, mm = (w >> 1) / jc;
+      const int m = mm ? pr.m2 : pr.m1;
+      const int jn = jh0 + jj, j = hemi ? J - 1 - jn : jn;
+      C2<R>* dst = rb + (size_t)((mm * AN_JC + jj) * 2 + hemi) * rowst + c;
+      const C2<R>* src = afe + (((size_t)m * J + j) * K + k0) * AF_N + c;
+      if (wide) cp_async_16b(dst, src);
+      else cp_async_c2(dst, src);
+    }
+    cp_async_commit_group();
+  };
+  prefetch(0, 0);
+  int buf = 0;
   for (int jh0 = 0; jh0 < JH; jh0 += AN_JC) {
     const int jc = min(AN_JC, JH - jh0);
-    __syncthreads();
-    // stage sym/anti combinations of the 7 inputs
-    // one warp per (m, latitude pair): contiguous runs of kn * 7 values
-    const int nwarp = nt >> 5, wid = tid >> 5, lane = tid & 31;
-    const int rowlen = kn * AF_N;
-    for (int w = wid; w < nm * jc; w += nwarp) {
-      const int mm = w / jc, jj = w - mm * jc;
-      const int m = mm ? pr.m2 : pr.m1;
-      const int jn = jh0 + jj, js = J - 1 - jn;
-      const C2<R>* srcn = afe + (((size_t)m * J + jn) * K + k0) * AF_N;
-      const C2<R>* srcs = afe + (((size_t)m * J + js) * K + k0) * AF_N;
-      C2<R>* dst = xs + (((size_t)mm * AN_JC + jj) * KC) * AF_N * 2;
-      for (int c = lane; c < rowlen; c += 32) {
-        const C2<R> xn = srcn[c], xsouth = srcs[c];
-        dst[2 * c] = xn + xsouth;
-        dst[2 * c + 1] = xn - xsouth;
-      }
-    }
+    if (jh0 + AN_JC < JH) prefetch(jh0 + AN_JC, buf ^ 1);
+    else cp_async_commit_group();
+    cp_async_wait_one();
     __syncthreads();
     if (active) {
+      const C2<R>* rb = raw + buf * rawbuf;
       for (int jj = 0; jj < jc; ++jj) {
-        const C2<R>* x = xs + (((size_t)mi * AN_JC + jj) * KC + k) * AF_N * 2;
+        // north / south rows -> equatorially symmetric [0] and antisymmetric [1] parts
+        const C2<R>* xn = rb + (size_t)((mi * AN_JC + jj) * 2) * rowst + k * AF_N;
+        const C2<R>* xsth = xn + rowst;
+        C2<R> x[AF_N][2];
+#pragma unroll
+        for (int f = 0; f < AF_N; ++f) {
+          const C2<R> a = xn[f], b = xsth[f];
+          x[f][0] = a + b;
+          x[f][1] = a - b;
+        }
         const int jh = jh0 + jj;
 #pragma unroll
         for (int i = 0; i < NC; ++i) {
@@ -424,18 +466,20 @@ __global__ void k_anal(SD<R> d) {
           const R P = tp[r * JH + jh], H = th[r * JH + jh];
           const int ps = (i & 1);          // parity of (n - m): rows alternate
           const int hs = ps ^ 1;
-          cfma(acc[i][0], P, x[AF_FU * 2 + ps]);
-          cfma(acc[i][1], P, x[AF_FV * 2 + ps]);
-          cfma(acc[i][2], P, x[AF_KE * 2 + ps]);
-          cfma(acc[i][3], P, x[AF_T * 2 + ps]);
-          cfma(acc[i][4], P, x[AF_Q * 2 + ps]);
-          cfma(acc[i][5], H, x[AF_FU * 2 + hs]);
-          cfma(acc[i][6], H, x[AF_FV * 2 + hs]);
-          cfma(acc[i][7], H, x[AF_XV * 2 + hs]);
-          cfma(acc[i][8], H, x[AF_YV * 2 + hs]);
+          cfma(acc[i][0], P, x[AF_FU][ps]);
+          cfma(acc[i][1], P, x[AF_FV][ps]);
+          cfma(acc[i][2], P, x[AF_KE][ps]);
+          cfma(acc[i][3], P, x[AF_T][ps]);
+          cfma(acc[i][4], P, x[AF_Q][ps]);
+          cfma(acc[i][5], H, x[AF_FU][hs]);
+          cfma(acc[i][6], H, x[AF_FV][hs]);
+          cfma(acc[i][7], H, x[AF_XV][hs]);
+          cfma(acc[i][8], H, x[AF_YV][hs]);
         }
       }
     }
+    buf ^= 1;
+    __syncthreads();
   }
   if (active) {
     const size_t NS = d.NS;
@@ -460,7 +504,7 @@ __global__ void k_anal(SD<R> d) {
   // surface: wt_pi and pi(t - dt), one thread per row (first level chunk only)
   if (kc != 0) return;
   __syncthreads();
-  C2<R>* ss = xs;                                    // [2][JH][2 fields][2]
+  C2<R>* ss = raw;                                   // [2][JH][2 fields][2]
   for (int idx = tid; idx < nm * JH * 2; idx += nt) {
     const int f = idx % 2, jh = (idx / 2) % JH, mm = idx / (2 * JH);
     const int m = mm ? pr.m2 : pr.m1;
@@ -700,11 +744,23 @@ __global__ void k_colsum(SD<R> d) {
   d.sas[es + 3 * NS + idx] = sdv;
 }
 
+// Two adjacent complex values in one store (16 bytes in FP32; the six-field
+// rows of sf start on 16-byte boundaries).
+LBM_D void store_pair(C2<float>* o, C2<float> a, C2<float> b) {
+  *reinterpret_cast<float4*>(o) = make_float4(a.x, a.y, b.x, b.y);
+}
+LBM_D void store_pair(C2<double>* o, C2<double> a, C2<double> b) {
+  o[0] = a;
+  o[1] = b;
+}
+
 // =============================================================================
 // Legendre synthesis: state A -> sf, sfs, per (member, m-pair, level chunk)
 // =============================================================================
+constexpr int SY_THREADS = 320;
+
 template <typename R, int JG, int KC>
-__global__ void k_synth(SD<R> d) {
+__global__ void __launch_bounds__(SY_THREADS, 2) k_synth(SD<R> d) {
   const int p = blockIdx.x, e = blockIdx.y, kc = blockIdx.z;
   const int J = d.J, K = d.K, N = d.N, M = d.M, JH = J / 2, NS = d.NS;
   const int k0 = kc * KC, kn = min(KC, K - k0);
@@ -712,7 +768,7 @@ __global__ void k_synth(SD<R> d) {
   extern __shared__ unsigned char smraw[];
   R* tp = reinterpret_cast<R*>(smraw);                 // [NR][JH]
   R* th = tp + pr.NR * JH;
-  C2<R>* sv = reinterpret_cast<C2<R>*>(th + pr.NR * JH);    // [NR][KC][6]
+  C2<R>* sv = reinterpret_cast<C2<R>*>(th + pr.NR * JH);    // [NR][6][KC]
   const int tid = threadIdx.x, nt = blockDim.x;
   const int off1 = spec_offset(pr.m1, N), off2 = spec_offset(pr.m2, N);
   for (int idx = tid; idx < pr.NR * JH; idx += nt) {
@@ -729,13 +785,13 @@ __global__ void k_synth(SD<R> d) {
     const size_t o = (size_t)row * K + k0 + kk;
     const C2<R> vo = d.sa3[e3 + 0 * (size_t)NS * K + o], dv = d.sa3[e3 + 1 * (size_t)NS * K + o];
     const R il = d.invlap[n];
-    C2<R>* s = sv + ((size_t)r * KC + kk) * 6;
-    s[0] = vo * il;                                    // psi
-    s[1] = dv * il;                                    // chi
-    s[2] = vo;
-    s[3] = dv;
-    s[4] = d.sa3[e3 + 2 * (size_t)NS * K + o];
-    s[5] = d.sa3[e3 + 3 * (size_t)NS * K + o];
+    C2<R>* s = sv + (size_t)r * 6 * KC + kk;         // field f at s[f * KC]
+    s[0 * KC] = vo * il;                               // psi
+    s[1 * KC] = dv * il;                               // chi
+    s[2 * KC] = vo;
+    s[3 * KC] = dv;
+    s[4 * KC] = d.sa3[e3 + 2 * (size_t)NS * K + o];
+    s[5 * KC] = d.sa3[e3 + 3 * (size_t)NS * K + o];
   }
   __syncthreads();
   const int NJG = (JH + JG - 1) / JG;
@@ -761,8 +817,9 @@ __global__ void k_synth(SD<R> d) {
     // symmetric about the equator (plus), H of an even row antisymmetric.
     auto row = [&](int r, auto par_tag) {
       constexpr int PP = decltype(par_tag)::value, HP = PP ^ 1;
-      const C2<R>* s = sv + ((size_t)r * KC + kk) * 6;
-      const C2<R> psi = s[0], chi = s[1], vo = s[2], dv = s[3], tt = s[4], qq = s[5];
+      const C2<R>* s = sv + (size_t)r * 6 * KC + kk;
+      const C2<R> psi = s[0 * KC], chi = s[1 * KC], vo = s[2 * KC], dv = s[3 * KC];
+      const C2<R> tt = s[4 * KC], qq = s[5 * KC];
 #pragma unroll
       for (int a = 0; a < JG; ++a) {
         const int jh = min(jg * JG + a, JH - 1);
@@ -792,12 +849,9 @@ __global__ void k_synth(SD<R> d) {
         const R sg = hemi ? R(-1) : R(1);
         auto comb = [&](int b) { return acc[a][b][0] + acc[a][b][1] * sg; };
         C2<R>* o = sfe + (((size_t)m * J + j) * K + k0 + kk) * SF_N;
-        o[SF_U] = im_mul(comb(0), rm) - comb(1);
-        o[SF_V] = im_mul(comb(2), rm) + comb(3);
-        o[SF_VOR] = comb(4);
-        o[SF_DIV] = comb(5);
-        o[SF_T] = comb(6);
-        o[SF_Q] = comb(7);
+        store_pair(o + SF_U, im_mul(comb(0), rm) - comb(1), im_mul(comb(2), rm) + comb(3));
+        store_pair(o + SF_VOR, comb(4), comb(5));
+        store_pair(o + SF_T, comb(6), comb(7));
       }
     }
    }
@@ -893,9 +947,8 @@ template <typename R, int I> constexpr int grid_nt() {
 }
 
 template <typename R> size_t anal_smem(int NR, int JH) {
-  return sizeof(R) * 2 * (size_t)NR * JH +
-         sizeof(C2<R>) * (size_t)2 * AN_JC * Cfg<R>::KCA * AF_N * 2 +
-         sizeof(C2<R>) * 0;
+  return sizeof(R) * 2 * (size_t)NR * JH + 16 +
+         sizeof(C2<R>) * (size_t)2 * (2 * AN_JC * 2 * AF_N * Cfg<R>::KCA);
 }
 template <typename R> size_t synth_smem(int NR, int JH) {
   return sizeof(R) * 2 * (size_t)NR * JH + sizeof(C2<R>) * (size_t)NR * Cfg<R>::KCS * 6;
@@ -926,7 +979,7 @@ template <typename R, int I> int launch_step(const SD<R>& d, const lbm_step_ctl&
     const int nt = ((KC * G + 31) / 32) * 32;
     // the surface pass also needs 2 * JH * 2 staging elements
     size_t sm = anal_smem<R>(NRmax, JH);
-    const size_t sm2 = sizeof(R) * 2 * (size_t)NRmax * JH + sizeof(C2<R>) * (size_t)2 * JH * 2 * 2;
+    const size_t sm2 = sizeof(R) * 2 * (size_t)NRmax * JH + 16 + sizeof(C2<R>) * (size_t)2 * JH * 2 * 2;
     if (sm2 > sm) sm = sm2;
     k_anal<R, NC, KC><<<dim3(NP, d.E, (d.K + KC - 1) / KC), nt, sm, st>>>(d);
   }
@@ -937,7 +990,7 @@ template <typename R, int I> int launch_step(const SD<R>& d, const lbm_step_ctl&
     constexpr int JG = Cfg<R>::JG, KC = Cfg<R>::KCS;
     const int NJG = (JH + JG - 1) / JG;
     int nt = NJG * KC;
-    nt = nt > 512 ? 512 : ((nt + 31) / 32) * 32;
+    nt = nt > SY_THREADS ? SY_THREADS : ((nt + 31) / 32) * 32;
     k_synth<R, JG, KC><<<dim3(NP, d.E, (d.K + KC - 1) / KC), nt, synth_smem<R>(NRmax, JH), st>>>(d);
   }
   LBM_LAUNCH_CHECK();
@@ -955,7 +1008,7 @@ template <typename R, int I> void set_attrs(const SD<R>& d) {
                          (int)GridSmem<R, I, KB, NT>::bytes(d.M));
   }
   size_t sm = anal_smem<R>(NRmax, JH);
-  const size_t sm2 = sizeof(R) * 2 * (size_t)NRmax * JH + sizeof(C2<R>) * (size_t)2 * JH * 2 * 2;
+  const size_t sm2 = sizeof(R) * 2 * (size_t)NRmax * JH + 16 + sizeof(C2<R>) * (size_t)2 * JH * 2 * 2;
   if (sm2 > sm) sm = sm2;
   cudaFuncSetAttribute(k_anal<R, Cfg<R>::NC, Cfg<R>::KCA>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -1034,7 +1087,7 @@ template <typename R> int prime(const lbm_stepper_desc* desc, cudaStream_t st) {
   const int JH = d.J / 2, NRmax = d.N + 2, NP = (d.M + 1) / 2;
   const int NJG = (JH + JG - 1) / JG;
   int nt = NJG * KC;
-  nt = nt > 512 ? 512 : ((nt + 31) / 32) * 32;
+  nt = nt > SY_THREADS ? SY_THREADS : ((nt + 31) / 32) * 32;
   k_synth<R, JG, KC><<<dim3(NP, d.E, (d.K + KC - 1) / KC), nt, synth_smem<R>(NRmax, JH), st>>>(d);
   LBM_LAUNCH_CHECK();
   return LBM_OK;
