@@ -207,21 +207,31 @@ def build_model(E, precision, torch, days=1.0, seed=SEED, device="cuda"):
 
 
 def algorithmic_bytes(E, p):
-    """HBM bytes each stepper kernel must move per launch (p = bytes/real)."""
+    """HBM bytes each stepper kernel must move per launch (p = bytes/real):
+    every array it reads or writes once, per-member arrays times E, the shared
+    basic state once."""
     nlon, nlat, nmax = GRID
     M, J, I, K = nmax + 1, nlat, nlon, K_LEV
     NS = M * (M + 1) // 2
     c = 2 * p
-    shared_grid = p * (10 * J * K * I + J * (K + 1) * I + 5 * J * I)
+    shared_grid = p * (14 * J * K * I + J * (K + 1) * I + 5 * J * I)
     sf = c * M * J * (6 * K + 5)
     af = c * M * J * (7 * K + 2)
+    g6 = 4 * J * I * (6 + 6 * K)
+    g9 = 4 * J * I * (2 + 9 * K)
     st3 = c * 4 * NS * K
-    return {
-        "grid": E * (sf + af + 4 * p * J * I) + shared_grid,
+    out = {
         "anal": E * (af + c * (4 * NS * K + 2 * NS)),
         "implicit": E * (3 * st3 + c * 2 * NS + 2 * st3 + c * 4 * NS),
         "synth": E * (st3 + c * 4 * NS + sf),
     }
+    if p == 4:      # FP32: the grid-point part is three launches
+        out.update({"idft": E * (sf + g6),
+                    "alg": E * (g6 + g9 + 4 * p * J * I) + shared_grid,
+                    "fdft": E * (g9 + af)})
+    else:
+        out["grid"] = E * (sf + af + 4 * p * J * I) + shared_grid
+    return out
 
 
 def read_traffic(kernel, E):
@@ -293,7 +303,12 @@ def main():
     d = stp.desc()
     L = lib()
     sh = stream_handle(stp.stream)
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    # kernel ids of lbm_stepper_launch in step order
+    kids = [4, 5, 6, 1, 2, 3] if args.precision == "fp32" else [0, 1, 2, 3]
+    names = (["idft", "alg", "fdft"] if args.precision == "fp32" else ["grid"]) + \
+        ["anal", "implicit", "synth"]
+    nk = len(kids)
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(nk + 1)]
            for _ in range(args.steps)]
     if world > 1:
         dist.barrier()
@@ -304,19 +319,19 @@ def main():
             for s in range(args.steps):
                 ev = evs[s]
                 ev[0].record(stp.stream)
-                for kern in range(4):
+                for i, kern in enumerate(kids):
                     check(L.lbm_stepper_launch(C.byref(d), ctl, kern, sh), "launch")
-                    ev[kern + 1].record(stp.stream)
+                    ev[i + 1].record(stp.stream)
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall
     stp.pending_ps_mode = 2
     if world > 1:
         dist.barrier()
-    total_ms = evs[0][0].elapsed_time(evs[-1][4])
-    kern_ms = np.zeros(4)
+    total_ms = evs[0][0].elapsed_time(evs[-1][nk])
+    kern_ms = np.zeros(nk)
     for ev in evs:
-        for kern in range(4):
-            kern_ms[kern] += ev[kern].elapsed_time(ev[kern + 1])
+        for i in range(nk):
+            kern_ms[i] += ev[i].elapsed_time(ev[i + 1])
     kern_ms /= args.steps
     t_max = total_ms
     if world > 1:
@@ -370,7 +385,6 @@ def main():
     if rank == 0:
         p = 4 if args.precision == "fp32" else 8
         ab = algorithmic_bytes(E, p)
-        names = ["grid", "anal", "implicit", "synth"]
         top = int(np.argmax(kern_ms))
         peaks = {}
         try:
@@ -395,7 +409,7 @@ def main():
                        "parallelism": f"members sharded, {world} independent rank(s)"},
             "clocks": clk.summary(),
             "e2e": e2e,
-            "gpu_launches": 4 * args.steps,
+            "gpu_launches": nk * args.steps,
             "roofline": {"bound": "hbm", "kernel": names[top], "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": read_traffic(names[top], E),

@@ -185,6 +185,11 @@ int lbm_implicit_step(int prec, const lbm_implicit_args* a, void* stream);
  *   af   [E][M][J][K][7] cplx  weighted Fourier inputs of the analysis
  *   afs  [E][M][J][2] cplx     gt_pi, pi(t-dt)
  *   tend [E][4][NS][K] cplx, tends [E][2][NS] cplx   explicit tendencies
+ *   grid6 [E][J][6 + 6K][I] float (FP32 mode; NULL in FP64 mode): grid rows
+ *        pi, pi_x, pi_y, U-sum, V-sum, D-sum, then per level u, v, vor,
+ *        div, T, q (u and v divided by a cos)
+ *   grid9 [E][J][2 + 9K][I] float (FP32 mode): gt_pi, pi(t - dt), then per
+ *        level gt, xu, g, yu, fu, fv, ke, xv, yv
  *   symp, symh [NS][J/2]       P and H at the northern latitudes, packed rows
  *   tw [I] cplx; jfac [4][J]: gw, gwdel*coslat, 1/(a coslat), coslat
  *   vert [16][K+1]: see LBM_VERT_* below
@@ -223,6 +228,7 @@ typedef struct lbm_stepper_desc {
   const void *frc3, *frcs, *dft;
   void *sa3, *sas, *sb3, *psa, *psb;
   void *sf, *sfs, *af, *afs, *tend, *tends;
+  void *grid6, *grid9;
   int* err;
 } lbm_stepper_desc;
 
@@ -246,9 +252,12 @@ int lbm_stepper_run(const lbm_stepper_desc* d, const lbm_step_ctl* ctl,
                     int nsteps, void* stream);
 
 /* One kernel of one step, for per-kernel timing and profiling: kernel 0 =
- * grid-point tendency with the longitude FFTs, 1 = Legendre analysis,
+ * grid-point tendency with the longitude transforms, 1 = Legendre analysis,
  * 2 = implicit update, 3 = Legendre synthesis.  Launching 0..3 in order is
- * the same as lbm_stepper_run for that step. */
+ * the same as lbm_stepper_run for that step.  In FP32 mode kernel 0 is three
+ * launches, also available one by one: 4 = longitude synthesis (sf, sfs ->
+ * grid6), 5 = column algebra (grid6 -> grid9, grid ps), 6 = longitude
+ * analysis (grid9 -> af, afs); 4, 5, 6 in order equal 0. */
 int lbm_stepper_launch(const lbm_stepper_desc* d, const lbm_step_ctl* ctl,
                        int kernel, void* stream);
 
@@ -276,26 +285,28 @@ int lbm_graph_destroy(lbm_graph* g);
  *
  * lbm_stepper_run_noalloc is lbm_stepper_prime followed by lbm_stepper_run
  * (same kernels, same results) for callers that cannot allocate device
- * memory for the six intermediate buffers sf, sfs, af, afs, tend, tends: a
+ * memory for the intermediate buffers (sf, sfs, af, afs, tend, tends and the
+ * FP32 grid rows grid6, grid9): a
  * host that embeds the dynamical core behind an FFI and hands the library
  * only its state, operator and forcing buffers -- for instance because all of
  * its device memory belongs to another runtime's pool, or because cudaMalloc
  * and cudaFree synchronise the device in the middle of its time loop -- and
- * that does not want to keep those buffers (6.2 MiB per member at T42L20 in
- * FP32, twice that in FP64) alive between calls.
+ * that does not want to keep those buffers (15.8 MiB per member at T42L20 in
+ * FP32, 12.4 MiB in FP64) alive between calls.
  *
  * The intermediates come instead from one static device array of
  * LBM_NOALLOC_SCRATCH_BYTES, which every GPU that loads the library holds
  * until the process exits.  The call allocates nothing: no cudaMalloc, no
  * cudaFree, no allocating library routine.
- *   - d: as for lbm_stepper_run; its sf, sfs, af, afs, tend and tends are
- *     ignored (may be NULL).  Every other pointer is the caller's, and the
- *     state (sa3, sas, sb3, psa, psb, err) is updated in place.
+ *   - d: as for lbm_stepper_run; its sf, sfs, af, afs, tend, tends, grid6
+ *     and grid9 are ignored (may be NULL).  Every other pointer is the
+ *     caller's, and the state (sa3, sas, sb3, psa, psb, err) is updated in
+ *     place.
  *   - The call needs E * M * J * (13 K + 7) + E * NS * (4 K + 2) complex
- *     values (each buffer rounded up to 256 bytes); a case larger than
- *     LBM_NOALLOC_SCRATCH_BYTES is rejected with LBM_ERR_SCRATCH before
- *     anything is launched (at most 5 members at T42L20 in FP32, 2 in FP64;
- *     20 and 10 at T21L20).
+ *     values, plus E * J * I * (15 K + 8) floats in FP32 mode (each buffer
+ *     rounded up to 256 bytes); a case larger than LBM_NOALLOC_SCRATCH_BYTES
+ *     is rejected with LBM_ERR_SCRATCH before anything is launched (at most
+ *     2 members at T42L20 in FP32 or FP64; 8 and 10 at T21L20).
  *   - Each call first clears the part of the area it uses (cudaMemsetAsync
  *     on `stream`) and synthesises the current level into it, so nothing
  *     carries over from an earlier call: the state in d is all there is.

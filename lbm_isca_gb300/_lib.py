@@ -56,7 +56,7 @@ class StepperDesc(C.Structure):
                                      "lap", "invlap", "nn1a", "kv", "kd", "ktt", "kq", "ww",
                                      "tmtx", "minv", "vdiff", "frc3", "frcs", "dft", "sa3", "sas",
                                      "sb3", "psa", "psb", "sf", "sfs", "af", "afs", "tend",
-                                     "tends")]
+                                     "tends", "grid6", "grid9")]
                 + [("err", C.POINTER(I32))])
 
 

@@ -46,6 +46,7 @@ template <typename R> struct SD {
   C2<R> *sa3, *sas, *sb3;
   R *psa, *psb;
   C2<R> *sf, *sfs, *af, *afs, *tend, *tends;
+  float *grid6, *grid9;
   int* err;
 };
 
@@ -69,6 +70,7 @@ template <typename R> SD<R> make_sd(const lbm_stepper_desc& d) {
   s.psa = (R*)d.psa; s.psb = (R*)d.psb;
   s.sf = (C2<R>*)d.sf; s.sfs = (C2<R>*)d.sfs; s.af = (C2<R>*)d.af; s.afs = (C2<R>*)d.afs;
   s.tend = (C2<R>*)d.tend; s.tends = (C2<R>*)d.tends;
+  s.grid6 = (float*)d.grid6; s.grid9 = (float*)d.grid9;
   s.err = d.err;
   return s;
 }
@@ -934,6 +936,7 @@ __global__ void k_ps_flush(SD<R> d, int ps_mode) {
 
 }  // namespace lbm
 #include "grid_dft.cuh"
+#include "grid_split.cuh"
 namespace lbm {
 
 // ---- launch configuration ------------------------------------------------------
@@ -965,13 +968,19 @@ template <typename R, int I> int launch_step(const SD<R>& d, const lbm_step_ctl&
   const int JH = d.J / 2;
   const int NRmax = d.N + 2;
   const size_t gsm = GridSmem<R, I, KB, NT>::bytes(d.M);
-  if (only < 0 || only == 0) {
-    if constexpr (sizeof(R) == 4) {
-      const size_t dsm = sizeof(float) * (size_t)DftLayout(I, d.M, d.K, DftGrid<I>::KB).total;
-      k_grid_dft<I><<<dim3(d.J, d.E), DftGrid<I>::NT, dsm, st>>>(d, d.dft, c.ps_mode);
-    } else {
+  if constexpr (sizeof(R) == 4) {
+    // grid-point part as three launches: longitude synthesis, column
+    // algebra, longitude analysis (kernel ids 4, 5, 6; 0 = all three)
+    if (only < 0 || only == 0 || only == 4)
+      k_idft<I><<<dim3(d.J, d.E), SPLIT_NT, idft_smem(I, d.M), st>>>(d, d.dft);
+    if (only < 0 || only == 0 || only == 5)
+      k_alg<I><<<dim3(d.J, d.E), I, 0, st>>>(d, c.ps_mode);
+    if (only < 0 || only == 0 || only == 6)
+      k_fdft<I><<<dim3(d.J, d.E), SPLIT_NT,
+                  sizeof(float) * (size_t)FdftLayout(I, d.M, DftGrid<I>::KB).total, st>>>(d, d.dft);
+  } else {
+    if (only < 0 || only == 0)
       k_grid<R, I, KB, NT><<<dim3(d.J, d.E), NT, gsm, st>>>(d, c.ps_mode);
-    }
   }
   if (only < 0 || only == 1) {
     constexpr int NC = Cfg<R>::NC, KC = Cfg<R>::KCA;
@@ -1001,8 +1010,10 @@ template <typename R, int I> void set_attrs(const SD<R>& d) {
   constexpr int KB = grid_kb<R, I>(), NT = grid_nt<R, I>();
   const int JH = d.J / 2, NRmax = d.N + 2;
   if constexpr (sizeof(R) == 4) {
-    cudaFuncSetAttribute(k_grid_dft<I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(sizeof(float) * DftLayout(I, d.M, d.K, DftGrid<I>::KB).total));
+    cudaFuncSetAttribute(k_idft<I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)idft_smem(I, d.M));
+    cudaFuncSetAttribute(k_fdft<I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(sizeof(float) * FdftLayout(I, d.M, DftGrid<I>::KB).total));
   } else {
     cudaFuncSetAttribute(k_grid<R, I, KB, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)GridSmem<R, I, KB, NT>::bytes(d.M));
@@ -1030,9 +1041,10 @@ template <typename R> int validate(const SD<R>& d) {
     return LBM_ERR_ARG;
   for (int f = 0; f < 4; ++f)
     if (d.vd_on[f] && !d.vdiff) return LBM_ERR_ARG;
-  if (sizeof(R) == 4 && !d.dft) return LBM_ERR_ARG;
+  if (sizeof(R) == 4 && (!d.dft || !d.grid6 || !d.grid9)) return LBM_ERR_ARG;
   if (sizeof(R) == 4 &&
-      sizeof(float) * (size_t)DftLayout(d.I, d.M, d.K, d.I == 256 ? 2 : 4).total > 227 * 1024)
+      (idft_smem(d.I, d.M) > 227 * 1024 ||
+       sizeof(float) * (size_t)FdftLayout(d.I, d.M, d.I == 256 ? 2 : 4).total > 227 * 1024))
     return LBM_ERR_ARG;
   return LBM_OK;
 }
@@ -1116,9 +1128,9 @@ template <typename R> int flush(const lbm_stepper_desc* desc, int ps_mode, cudaS
 }
 
 // ---- stepping from a static scratch area ------------------------------------
-// lbm_stepper_run_noalloc takes the six intermediate buffers of a step (sf,
-// sfs, af, afs, tend, tends) from this file-scope array instead of caller
-// memory.  It is sized once, at LBM_NOALLOC_SCRATCH_BYTES, and every GPU that
+// lbm_stepper_run_noalloc takes the intermediate buffers of a step (sf, sfs,
+// af, afs, tend, tends and in FP32 mode grid6, grid9) from this file-scope
+// array instead of caller memory.  It is sized once, at LBM_NOALLOC_SCRATCH_BYTES, and every GPU that
 // loads the library holds it until the process exits.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[LBM_NOALLOC_SCRATCH_BYTES];
 
@@ -1126,19 +1138,22 @@ constexpr int NOALLOC_MAX_DEVICES = 64;
 static std::mutex g_noalloc_mu;
 static void* g_noalloc_base[NOALLOC_MAX_DEVICES];
 
-// Byte offsets of sf, sfs, af, afs, tend, tends in the scratch area, each
-// rounded up to 256 bytes.  `need` is the total, computed in double so that
-// an absurd size cannot wrap around before it is compared with the maximum.
-static void noalloc_layout(const lbm_stepper_desc& d, size_t off[6], double* need) {
+// Byte offsets of sf, sfs, af, afs, tend, tends (and in FP32 mode grid6,
+// grid9) in the scratch area, each rounded up to 256 bytes.  `need` is the
+// total, computed in double so that an absurd size cannot wrap around before
+// it is compared with the maximum.
+static void noalloc_layout(const lbm_stepper_desc& d, size_t off[8], double* need) {
   const double c = 2.0 * (d.prec == LBM_F64 ? sizeof(double) : sizeof(float));
-  const double E = d.nmem, M = d.nmax + 1.0, J = d.nlat, K = d.kmax;
+  const double E = d.nmem, M = d.nmax + 1.0, J = d.nlat, K = d.kmax, I = d.nlon;
   const double NS = M * (M + 1.0) / 2.0;
-  const double n[6] = {E * M * J * K * 6, E * M * J * 5, E * M * J * K * 7,
-                       E * M * J * 2,     E * 4 * NS * K, E * 2 * NS};
+  const double g = (d.prec == LBM_F32) ? 1.0 : 0.0;
+  const double bytes[8] = {c * E * M * J * K * 6, c * E * M * J * 5, c * E * M * J * K * 7,
+                           c * E * M * J * 2,     c * E * 4 * NS * K, c * E * 2 * NS,
+                           g * 4.0 * E * J * (6 + 6 * K) * I, g * 4.0 * E * J * (2 + 9 * K) * I};
   double t = 0.0;
-  for (int i = 0; i < 6; ++i) {
+  for (int i = 0; i < 8; ++i) {
     off[i] = (size_t)t;
-    t += 256.0 * std::ceil(n[i] * c / 256.0);
+    t += 256.0 * std::ceil(bytes[i] / 256.0);
   }
   *need = t;
 }
@@ -1208,7 +1223,8 @@ int lbm_stepper_run(const lbm_stepper_desc* d, const lbm_step_ctl* ctl, int nste
 
 int lbm_stepper_launch(const lbm_stepper_desc* d, const lbm_step_ctl* ctl, int kernel,
                        void* stream) {
-  if (!d || !ctl || kernel < 0 || kernel > 3 || (d->prec != LBM_F64 && d->prec != LBM_F32))
+  if (!d || !ctl || kernel < 0 || kernel > 6 || (d->prec != LBM_F64 && d->prec != LBM_F32) ||
+      (kernel > 3 && d->prec != LBM_F32))
     return LBM_ERR_ARG;
   int rc = d->prec == LBM_F64 ? prepare_attrs<double>(d) : prepare_attrs<float>(d);
   if (rc) return rc;
@@ -1279,7 +1295,7 @@ int lbm_stepper_run_noalloc(const lbm_stepper_desc* d, const lbm_step_ctl* ctl, 
                             void* stream) {
   if (!d || !ctl || nsteps < 0 || (d->prec != LBM_F64 && d->prec != LBM_F32)) return LBM_ERR_ARG;
   if (d->nmem < 1 || d->nlat < 2 || d->nmax < 1 || d->kmax < 1) return LBM_ERR_ARG;
-  size_t off[6];
+  size_t off[8];
   double need = 0.0;
   noalloc_layout(*d, off, &need);
   if (need > (double)LBM_NOALLOC_SCRATCH_BYTES) return LBM_ERR_SCRATCH;
@@ -1298,6 +1314,8 @@ int lbm_stepper_run_noalloc(const lbm_stepper_desc* d, const lbm_step_ctl* ctl, 
   w.afs = b + off[3];
   w.tend = b + off[4];
   w.tends = b + off[5];
+  w.grid6 = d->prec == LBM_F32 ? b + off[6] : nullptr;
+  w.grid9 = d->prec == LBM_F32 ? b + off[7] : nullptr;
   const size_t clear = (size_t)need;
   cudaStream_t st = (cudaStream_t)stream;
   return d->prec == LBM_F64 ? run_noalloc<double>(w, ctl, nsteps, clear, st)

@@ -113,6 +113,13 @@ class EnsembleStepper:
         self.sf, self.sfs = z(E, M, J, K, 6), z(E, M, J, 5)
         self.af, self.afs = z(E, M, J, K, 7), z(E, M, J, 2)
         self.tend, self.tends = z(E, 4, NS, K), z(E, 2, NS)
+        # FP32 grid rows between the longitude transforms and the column algebra
+        if precision == "fp32":
+            f = lambda *s_: torch.zeros(s_, device=dev, dtype=torch.float32)   # noqa: E731
+            self.grid6 = f(E, J, 6 + 6 * K, I)
+            self.grid9 = f(E, J, 2 + 9 * K, I)
+        else:
+            self.grid6 = self.grid9 = None
         self.err = torch.zeros(1, device=dev, dtype=torch.int32)
         self.frc3 = self.frcs = None
         self.frc_shared = 1
@@ -230,7 +237,7 @@ class EnsembleStepper:
         d.kappa, d.epsvt, d.robert = KAPPA, EPSVT, self.robert
         for name in ("symp", "symh", "tw", "jfac", "vert", "b3", "bsd", "b2", "lap", "invlap",
                      "nn1a", "kv", "kd", "ktt", "kq", "ww", "tmtx", "sa3", "sas", "sb3", "psa",
-                     "psb", "sf", "sfs", "af", "afs", "tend", "tends"):
+                     "psb", "sf", "sfs", "af", "afs", "tend", "tends", "grid6", "grid9"):
             setattr(d, name, ptr(getattr(self, name)))
         d.minv = ptr(self.minv)
         d.vdiff = ptr(self.vdm)

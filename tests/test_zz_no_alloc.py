@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 DT = 1200.0            # T21: 72 steps a day
 TOL = {"fp64": 1e-12, "fp32": 1e-6}
-SCRATCH = ("sf", "sfs", "af", "afs", "tend", "tends")
+SCRATCH = ("sf", "sfs", "af", "afs", "tend", "tends", "grid6", "grid9")
 STATE = ("sa3", "sas", "sb3", "psa", "psb")
 
 
