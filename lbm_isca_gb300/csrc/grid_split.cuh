@@ -14,7 +14,7 @@
 //   k_fdft  per (latitude, member): the weighted longitude analysis of grid9
 //           -> af/afs.
 //
-// The DFTs use the same quarter-wave folding and tables as k_grid_dft.
+// The DFTs use the quarter-wave folding of grid_dft.cuh.
 
 namespace lbm {
 
@@ -292,110 +292,186 @@ __global__ void __launch_bounds__(I) k_alg(SD<float> d, int ps_mode) {
 }
 
 // ---------------------------------------------------------------------------
+// Longitude analysis.  A chunk of LC levels at a time: the 9 LC grid rows
+// (and in the first chunk the two surface rows) stream into shared memory by
+// cp.async while the previous chunk computes, are folded by quarter-wave
+// symmetry into fw[row][i] = (u+uh, u-uh, v-vh, v+vh) (u, v: sum / difference
+// of x_i and x_{I-i}; uh, vh: of x_{I/2-i} and x_{I/2+i}), and each thread
+// item accumulates one "quad" of 4 rows against one wavenumber pair (m even,
+// m odd), reading one packed table entry (cos, sin of the even m, cos, sin of
+// the odd m) per point.
+LBM_HD int fdft_quads(int lc) { return 2 * lc + (lc + 3) / 4; }
+
 struct FdftLayout {
-  int tab, gin, fw, fout, total;     // float units
+  int tab, raw, fw, fout, total;     // float units, 16-byte aligned blocks
   LBM_HD static int al4(int x) { return (x + 3) & ~3; }
-  LBM_HD FdftLayout(int I, int M, int KB) {
-    const int Q = I / 4;
+  LBM_HD FdftLayout(int I, int M, int LC) {
+    const int Q = I / 4, NP = (M + 1) / 2, NR = 9 * LC + 2;
     int o = 0;
-    tab = o; o = al4(o + 2 * M * (Q + 1));
-    gin = o; o = al4(o + 2 * KB * 9 * I);            // two buffers [KB*9][I]
-    fw = o; o = al4(o + KB * 9 * (Q + 1) * 4);
-    fout = o; o = al4(o + 2 * KB * 7 * M);
+    tab = o; o = al4(o + 4 * NP * (Q + 1));
+    raw = o; o = al4(o + NR * I);
+    fw = o; o = al4(o + 4 * NR * (Q + 1));
+    fout = o; o = al4(o + 2 * LC * AF_N * M);
     total = o;
   }
 };
 
+// Level chunk: as many levels as keep the thread items of a chunk within one
+// pass of the block and the shared memory within 74 KB (three CTAs on an SM),
+// then evened out over the chunks.
+LBM_HD int fdft_chunk(int I, int M, int K) {
+  const int NP = (M + 1) / 2;
+  int lc = K;
+  while (lc > 1 && ((fdft_quads(lc) + 1) * NP > SPLIT_NT ||
+                    sizeof(float) * (size_t)FdftLayout(I, M, lc).total > 74 * 1024))
+    --lc;
+  const int nchunk = (K + lc - 1) / lc;
+  return (K + nchunk - 1) / nchunk;
+}
+
 template <int I>
-__global__ void __launch_bounds__(SPLIT_NT) k_fdft(SD<float> d, const float2* __restrict__ dft) {
-  constexpr int Q = I / 4, NT = SPLIT_NT, NW = NT / 32, KB = DftGrid<I>::KB, NG = 9;
+__global__ void __launch_bounds__(SPLIT_NT) k_fdft(SD<float> d, const float2* __restrict__ dft,
+                                                  int LC) {
+  constexpr int Q = I / 4, NT = SPLIT_NT, NW = NT / 32;
   const int j = blockIdx.x, e = blockIdx.y;
-  const int J = d.J, K = d.K, M = d.M;
+  const int J = d.J, K = d.K, M = d.M, NP = (M + 1) / 2;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const FdftLayout L(I, M, KB);
+  const FdftLayout L(I, M, LC);
   extern __shared__ float4 sm4[];
   float* sm = reinterpret_cast<float*>(sm4);
-  float2* tab = reinterpret_cast<float2*>(sm + L.tab);
-  float* gin = sm + L.gin;
-  float4* fw = reinterpret_cast<float4*>(sm + L.fw);
-  float2* fout = reinterpret_cast<float2*>(sm + L.fout);
-  for (int x = tid; x < M * (Q + 1); x += NT) tab[x] = dft[x];
+  float4* tab = reinterpret_cast<float4*>(sm + L.tab);     // [NP][Q+1]
+  float* raw = sm + L.raw;                                 // [rows][I]
+  float4* fw = reinterpret_cast<float4*>(sm + L.fw);       // [rows][Q+1]
+  float2* fout = reinterpret_cast<float2*>(sm + L.fout);   // [LC*7][M]
+  for (int x = tid; x < NP * (Q + 1); x += NT) {
+    const int p = x / (Q + 1), i = x - p * (Q + 1);
+    const float2 te = dft[(2 * p) * (Q + 1) + i];
+    const float2 to = (2 * p + 1 < M) ? dft[(2 * p + 1) * (Q + 1) + i] : make_float2(0.f, 0.f);
+    tab[x] = make_float4(te.x, te.y, to.x, to.y);
+  }
   const float gw = d.jfac[JF_GW * J + j], gwdc = d.jfac[JF_GWDELC * J + j];
   const float wg = gw / float(I), wd = gwdc / float(I);
   const float* g9 = d.grid9 + ((size_t)e * J + j) * fdft_rows(K) * I;
   float2* afe = reinterpret_cast<float2*>(d.af) + (size_t)e * M * J * K * AF_N;
-  // level rows of levels k0 .. k0 + kb - 1 into buffer b (16-byte copies)
-  auto stage = [&](int k0, int b) {
-    const int kb = min(KB, K - k0);
-    float* G = gin + (size_t)b * KB * NG * I;
-    const float* src = g9 + (size_t)(2 + k0 * NG) * I;
-    const int n4 = kb * NG * I / 4;
-    for (int x = tid; x < n4; x += NT) cp_async16(G + 4 * x, src + 4 * x);
+  // rows of the chunk at k0: level rows 0 .. 9 lc - 1, then (first chunk)
+  // the two surface rows
+  auto stage = [&](int k0) {
+    const int lc = min(LC, K - k0);
+    const float* src = g9 + (size_t)(2 + 9 * k0) * I;
+    const int n4 = 9 * lc * I / 4;
+    for (int x = tid; x < n4; x += NT) cp_async16(raw + 4 * x, src + 4 * x);
+    if (k0 == 0)
+      for (int x = tid; x < 2 * I / 4; x += NT) cp_async16(raw + 9 * lc * I + 4 * x, g9 + 4 * x);
     cp_async_commit();
   };
-  stage(0, 0);
-
-  // surface rows: wt_pi and pi(t - dt)
-  {
-    float* G = gin + (size_t)KB * NG * I;             // buffer 1, free until level 1
-    for (int x = tid; x < 2 * I; x += NT) G[x] = g9[x];
+  stage(0);
+  for (int k0 = 0; k0 < K; k0 += LC) {
+    const int lc = min(LC, K - k0);
+    const bool surf = (k0 == 0);
+    const int nrow = 9 * lc + (surf ? 2 : 0);
+    cp_async_wait<0>();
     __syncthreads();
-    dft_fold<I>(fw, 2, G);
+    for (int x = tid; x < nrow * (Q + 1); x += NT) {
+      const int r = x / (Q + 1), i = x - r * (Q + 1);
+      const float* row = raw + (size_t)r * I;
+      float4 v;
+      if (i == 0) {
+        const float xq = row[Q], x3q = row[3 * Q];
+        v = make_float4(row[0], row[I / 2], xq + x3q, xq - x3q);
+      } else if (i == Q) {
+        v = make_float4(0.f, 0.f, 0.f, 0.f);
+      } else {
+        const float xa = row[i], xb = row[I - i], xc = row[I / 2 - i], xd = row[I / 2 + i];
+        const float u = xa + xb, w = xa - xb, uh = xc + xd, vh = xc - xd;
+        v = make_float4(u + uh, u - uh, w - vh, w + vh);
+      }
+      fw[x] = v;
+    }
     __syncthreads();
-    dft_forward<I>(tab, fw, 1, M, [](int q, int k) { return k < 2 ? k : -1; },
-                   [&](int q, int m, const int* fi, const float2* X) {
-                     float2* o = reinterpret_cast<float2*>(d.afs) + (((size_t)e * M + m) * J + j) * 2;
-                     o[0] = make_float2(X[0].x * wg, X[0].y * wg);
-                     o[1] = make_float2(X[1].x * wg, X[1].y * wg);
-                   });
-    __syncthreads();
-  }
-
-  int buf = 0;
-  for (int k0 = 0; k0 < K; k0 += KB) {
-    const int kb = min(KB, K - k0);
-    if (k0 + KB < K) stage(k0 + KB, buf ^ 1);
-    else cp_async_commit();
-    cp_async_wait<1>();
-    __syncthreads();
-    dft_fold<I>(fw, kb * NG, gin + (size_t)buf * KB * NG * I);
-    __syncthreads();
-    // quads: 2l -> (gt, xu, g, yu) of level l; 2l+1 -> (fu, fv, ke, xv); 2kb -> yv's
-    dft_forward<I>(
-        tab, fw, 2 * kb + 1, M,
-        [&](int q, int k) -> int {
-          if (q < 2 * kb) return (q >> 1) * NG + ((q & 1) ? 4 + k : k);
-          return k < kb ? k * NG + 8 : -1;
-        },
-        [&](int q, int m, const int* fi, const float2* X) {
-          const float rm = float(m);
-          if (q < 2 * kb) {
-            const int l = q >> 1;
-            float2* o = fout + (size_t)(l * AF_N) * M;
-            if ((q & 1) == 0) {
-              // a3 = wg X(gt) - wd i m X(xu); a5 = wg X(g) - wd i m X(yu)
-              o[AF_T * M + m] = make_float2(wg * X[0].x + wd * rm * X[1].y,
-                                            wg * X[0].y - wd * rm * X[1].x);
-              o[AF_Q * M + m] = make_float2(wg * X[2].x + wd * rm * X[3].y,
-                                            wg * X[2].y - wd * rm * X[3].x);
-            } else {
-              o[AF_FU * M + m] = make_float2(wd * X[0].x, wd * X[0].y);
-              o[AF_FV * M + m] = make_float2(wd * X[1].x, wd * X[1].y);
-              o[AF_KE * M + m] = make_float2(wg * X[2].x, wg * X[2].y);
-              o[AF_XV * M + m] = make_float2(wd * X[3].x, wd * X[3].y);
-            }
+    if (k0 + LC < K) stage(k0 + LC);             // next chunk streams in meanwhile
+    const int nq = fdft_quads(lc) + (surf ? 1 : 0);
+    for (int it = tid; it < nq * NP; it += NT) {
+      const int p = it % NP, q = it / NP;
+      // rows of quad q (-1: none)
+      int rw[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        if (q < 2 * lc) {
+          rw[t] = 9 * (q >> 1) + ((q & 1) ? 4 : 0) + t;
+        } else if (q < fdft_quads(lc)) {
+          const int l = 4 * (q - 2 * lc) + t;
+          rw[t] = l < lc ? 9 * l + 8 : -1;
+        } else {
+          rw[t] = t < 2 ? 9 * lc + t : -1;
+        }
+      }
+      const float4* w[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) w[t] = fw + (size_t)(rw[t] >= 0 ? rw[t] : 0) * (Q + 1);
+      float acc[4][4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
+      const float4* tb = tab + (size_t)p * (Q + 1);
+#pragma unroll 4
+      for (int i = 1; i < Q; ++i) {
+        const float4 c = tb[i];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const float4 a = w[t][i];
+          acc[t][0] = fmaf(a.x, c.x, acc[t][0]);   // even m: cos
+          acc[t][1] = fmaf(a.z, c.y, acc[t][1]);   // even m: sin
+          acc[t][2] = fmaf(a.y, c.z, acc[t][2]);   // odd m: cos
+          acc[t][3] = fmaf(a.w, c.w, acc[t][3]);   // odd m: sin
+        }
+      }
+      const int me = 2 * p, mo = 2 * p + 1;
+      const float ce = (p & 1) ? -1.f : 1.f;            // (-1)^{me/2}
+      const float so = (((mo - 1) / 2) & 1) ? -1.f : 1.f;  // (-1)^{(mo-1)/2}
+      float2 Xe[4], Xo[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const float4 b0 = w[t][0];        // (x0, x_{I/2}, u_Q, v_Q)
+        Xe[t] = make_float2(acc[t][0] + b0.x + b0.y + ce * b0.z, -acc[t][1]);
+        Xo[t] = make_float2(acc[t][2] + b0.x - b0.y, -(acc[t][3] + so * b0.w));
+      }
+      // I X_m of the quad's rows -> weighted analysis inputs
+      for (int par = 0; par < 2; ++par) {
+        const int m = par ? mo : me;
+        if (m >= M) break;
+        const float2* X = par ? Xo : Xe;
+        const float rm = float(m);
+        if (q < 2 * lc) {
+          float2* o = fout + (size_t)((q >> 1) * AF_N) * M;
+          if ((q & 1) == 0) {
+            // a3 = wg X(gt) - wd i m X(xu); a5 = wg X(g) - wd i m X(yu)
+            o[AF_T * M + m] = make_float2(wg * X[0].x + wd * rm * X[1].y,
+                                          wg * X[0].y - wd * rm * X[1].x);
+            o[AF_Q * M + m] = make_float2(wg * X[2].x + wd * rm * X[3].y,
+                                          wg * X[2].y - wd * rm * X[3].x);
           } else {
-            for (int k = 0; k < kb; ++k)
-              fout[(size_t)(k * AF_N + AF_YV) * M + m] = make_float2(wd * X[k].x, wd * X[k].y);
+            o[AF_FU * M + m] = make_float2(wd * X[0].x, wd * X[0].y);
+            o[AF_FV * M + m] = make_float2(wd * X[1].x, wd * X[1].y);
+            o[AF_KE * M + m] = make_float2(wg * X[2].x, wg * X[2].y);
+            o[AF_XV * M + m] = make_float2(wd * X[3].x, wd * X[3].y);
           }
-        });
+        } else if (q < fdft_quads(lc)) {
+          for (int t = 0; t < 4; ++t) {
+            const int l = 4 * (q - 2 * lc) + t;
+            if (l < lc) fout[(size_t)(l * AF_N + AF_YV) * M + m] = make_float2(wd * X[t].x, wd * X[t].y);
+          }
+        } else {
+          float2* o = reinterpret_cast<float2*>(d.afs) + (((size_t)e * M + m) * J + j) * 2;
+          o[0] = make_float2(X[0].x * wg, X[0].y * wg);
+          o[1] = make_float2(X[1].x * wg, X[1].y * wg);
+        }
+      }
+    }
     __syncthreads();
-    const int row = kb * AF_N;
+    const int row = lc * AF_N;
     for (int m = warp; m < M; m += NW) {
       float2* dst = afe + ((size_t)m * J + j) * K * AF_N + (size_t)k0 * AF_N;
       for (int c = lane; c < row; c += 32) dst[c] = fout[c * M + m];
     }
-    buf ^= 1;
   }
 }
 

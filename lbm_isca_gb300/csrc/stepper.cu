@@ -975,9 +975,11 @@ template <typename R, int I> int launch_step(const SD<R>& d, const lbm_step_ctl&
       k_idft<I><<<dim3(d.J, d.E), SPLIT_NT, idft_smem(I, d.M), st>>>(d, d.dft);
     if (only < 0 || only == 0 || only == 5)
       k_alg<I><<<dim3(d.J, d.E), I, 0, st>>>(d, c.ps_mode);
-    if (only < 0 || only == 0 || only == 6)
-      k_fdft<I><<<dim3(d.J, d.E), SPLIT_NT,
-                  sizeof(float) * (size_t)FdftLayout(I, d.M, DftGrid<I>::KB).total, st>>>(d, d.dft);
+    if (only < 0 || only == 0 || only == 6) {
+      const int lc = fdft_chunk(I, d.M, d.K);
+      k_fdft<I><<<dim3(d.J, d.E), SPLIT_NT, sizeof(float) * (size_t)FdftLayout(I, d.M, lc).total,
+                  st>>>(d, d.dft, lc);
+    }
   } else {
     if (only < 0 || only == 0)
       k_grid<R, I, KB, NT><<<dim3(d.J, d.E), NT, gsm, st>>>(d, c.ps_mode);
@@ -1013,7 +1015,7 @@ template <typename R, int I> void set_attrs(const SD<R>& d) {
     cudaFuncSetAttribute(k_idft<I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)idft_smem(I, d.M));
     cudaFuncSetAttribute(k_fdft<I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(sizeof(float) * FdftLayout(I, d.M, DftGrid<I>::KB).total));
+                         (int)(sizeof(float) * FdftLayout(I, d.M, fdft_chunk(I, d.M, d.K)).total));
   } else {
     cudaFuncSetAttribute(k_grid<R, I, KB, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)GridSmem<R, I, KB, NT>::bytes(d.M));
@@ -1044,7 +1046,7 @@ template <typename R> int validate(const SD<R>& d) {
   if (sizeof(R) == 4 && (!d.dft || !d.grid6 || !d.grid9)) return LBM_ERR_ARG;
   if (sizeof(R) == 4 &&
       (idft_smem(d.I, d.M) > 227 * 1024 ||
-       sizeof(float) * (size_t)FdftLayout(d.I, d.M, d.I == 256 ? 2 : 4).total > 227 * 1024))
+       sizeof(float) * (size_t)FdftLayout(d.I, d.M, fdft_chunk(d.I, d.M, d.K)).total > 227 * 1024))
     return LBM_ERR_ARG;
   return LBM_OK;
 }
