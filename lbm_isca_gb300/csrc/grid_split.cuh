@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(SPLIT_NT) k_idft(SD<float> d, const float2* __
   const int j = blockIdx.x, e = blockIdx.y;
   const int J = d.J, K = d.K, M = d.M;
   const int NR = idft_rows(K);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tid = threadIdx.x;
   extern __shared__ float4 sm4[];
   float2* tab = reinterpret_cast<float2*>(sm4);                       // [M][Q+1]
   float2* fin = reinterpret_cast<float2*>(
@@ -143,25 +143,18 @@ __global__ void __launch_bounds__(SPLIT_NT) k_idft(SD<float> d, const float2* __
         row[I / 2 + i] = (mn - dd) * sc;
       }
     }
-    // i = 0 and i = I/2: lane-parallel sums, one warp per row
-    for (int r = warp; r < nr; r += NT / 32) {
-      float s0 = 0.f, s1 = 0.f;
-      for (int m = 1 + lane; m < M; m += 32) {
+    // i = 0 and i = I/2: one row per thread (consecutive rows, no bank conflicts)
+    for (int r = tid; r < nr; r += NT) {
+      float se_ = 0.f, so_ = 0.f;
+      for (int m = 1; m < M; ++m) {
         const float a = F[(size_t)m * RC + r].x;
-        s0 += a;
-        s1 += (m & 1) ? -a : a;
+        if (m & 1) so_ += a;
+        else se_ += a;
       }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
-        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-      }
-      if (lane == 0) {
-        const int v = v0 + r;
-        const float sc = rscale(v), x0 = F[r].x;
-        g6[(size_t)v * I] = (x0 + 2.f * s0) * sc;
-        g6[(size_t)v * I + I / 2] = (x0 + 2.f * s1) * sc;
-      }
+      const int v = v0 + r;
+      const float sc = rscale(v), x0 = F[r].x;
+      g6[(size_t)v * I] = (x0 + 2.f * (se_ + so_)) * sc;
+      g6[(size_t)v * I + I / 2] = (x0 + 2.f * (se_ - so_)) * sc;
     }
     buf ^= 1;
     __syncthreads();
@@ -212,27 +205,29 @@ __global__ void __launch_bounds__(I) k_alg(SD<float> d, int ps_mode) {
   }
 
   // ---- levels, bottom up ----
-  const float* b3c = d.b3 + (size_t)j * K * I + c;
-  const size_t b3f = (size_t)J * K * I;
-  const float* bsdc = d.bsd + (size_t)j * (K + 1) * I + c;
-  auto LV = [&](int k, int f) { return g6[(size_t)(6 + k * SF_N + f) * I]; };
+  // per-field offsets into b3 (int: the basic state of one latitude is small)
+  const int b3f = J * K * I;
+  const float* bk = d.b3 + (size_t)j * K * I + c;             // level k, field 0
+  const float* bsk = d.bsd + (size_t)j * (K + 1) * I + c;     // interface k
+  const float* gl = g6 + (size_t)6 * I;                       // level k rows
+  float* go = g9 + (size_t)2 * I;
   float sdlo = (V(LBM_VERT_SIGM, 0) - 1.f) * stot;   // sigma-dot at k - 1/2
   float prefd = 0.f, prefp = 0.f, pref3 = 0.f;
   // level window: m = k-1, 0 = k, p = k+1 (u, v, T, q); vorticity and
   // divergence of level k only
   float um = 0.f, vm = 0.f, tm_ = 0.f, qm = 0.f;
-  float u0 = LV(0, SF_U), v0 = LV(0, SF_V), t0 = LV(0, SF_T), q0 = LV(0, SF_Q);
-  float vo0 = LV(0, SF_VOR), dv0 = LV(0, SF_DIV);
+  float u0 = gl[SF_U * I], v0 = gl[SF_V * I], t0 = gl[SF_T * I], q0 = gl[SF_Q * I];
+  float vo0 = gl[SF_VOR * I], dv0 = gl[SF_DIV * I];
   float hum = 0.f, hvm = 0.f, htm = 0.f, hqm = 0.f;    // half differences at k - 1
-  float sb0 = bsdc[0];
+  float sb0 = __ldg(bsk);
   for (int k = 0; k < K; ++k) {
     const bool hasm = k >= 1, hasp = k + 1 <= K - 1;
     float up = u0, vp = v0, tp = t0, qp = q0, vop = 0.f, dvp = 0.f;
     if (hasp) {
-      up = LV(k + 1, SF_U); vp = LV(k + 1, SF_V); tp = LV(k + 1, SF_T); qp = LV(k + 1, SF_Q);
-      vop = LV(k + 1, SF_VOR); dvp = LV(k + 1, SF_DIV);
+      const float* gn = gl + SF_N * I;
+      up = gn[SF_U * I]; vp = gn[SF_V * I]; tp = gn[SF_T * I]; qp = gn[SF_Q * I];
+      vop = gn[SF_VOR * I]; dvp = gn[SF_DIV * I];
     }
-    const float* bk = b3c + (size_t)k * I;
     const float ub = __ldg(bk + B_U * b3f), vb = __ldg(bk + B_V * b3f);
     const float tb = __ldg(bk + B_T * b3f), qb = __ldg(bk + B_Q * b3f);
     const float tvb = __ldg(bk + B_TV * b3f), absv = __ldg(bk + B_ABSVOR * b3f);
@@ -240,8 +235,8 @@ __global__ void __launch_bounds__(I) k_alg(SD<float> d, int ps_mode) {
     const float tdev = __ldg(bk + B_TDEV * b3f), tvdev = __ldg(bk + B_TVDEV * b3f);
     const float hup = __ldg(bk + B_HDU * b3f), hvp = __ldg(bk + B_HDV * b3f);
     const float htp = __ldg(bk + B_HDT * b3f), hqp = __ldg(bk + B_HDQ * b3f);
-    const float sb1 = __ldg(bsdc + (size_t)(k + 1) * I);
-    const float dsk = V(LBM_VERT_DSIG, k);
+    const float sb1 = __ldg(bsk + I);
+    const float dsk = V(LBM_VERT_DSIG, k), rdsk = 1.f / dsk;
     // column scans through level k
     const float pa = u0 * pixb + ub * pix + v0 * piyb + vb * piy;      // v.grad(pi)
     const float sdup = sdlo + dsk * (dv0 + pa - stot);               // sigma-dot at k + 1/2
@@ -252,34 +247,39 @@ __global__ void __launch_bounds__(I) k_alg(SD<float> d, int ps_mode) {
     pref3 += V(LBM_VERT_RDLOG3, k) * xv;
     const float sdv = dh - prefd, spv = sx - prefp;                   // suffix sums above k
     const float sd0 = hasm ? sdlo : 0.f, sd1 = hasp ? sdup : 0.f;
+    // vertical advection in differences (vadv_p / vadv_b) times 1 / dsig_k:
+    // perturbation fields by the basic sigma-dot, basic fields by sigma-dot'
+    auto vp_ = [&](float fm, float f0, float fp) {
+      const float a = hasp ? 0.5f * sb1 * (fp - f0) : -sb1 * f0;
+      const float b = hasm ? 0.5f * sb0 * (f0 - fm) : sb0 * f0;
+      return (a + b) * rdsk;
+    };
+    auto vb_ = [&](float f0, float hm, float hp) {
+      const float a = hasp ? sd1 * hp : -sd1 * f0;
+      const float b = hasm ? sd0 * hm : sd0 * f0;
+      return (a + b) * rdsk;
+    };
     // temperature: adiabatic term and the reference-temperature matrix with
-    // Tref cancelled algebraically (see k_grid_dft)
-    const float tv = t0 + eps * (t0 * qb + tb * q0);
+    // Tref cancelled algebraically
+    const float tv = t0 + xv;
     const float al = V(LBM_VERT_ALPHA, k), w3 = V(LBM_VERT_W3, k);
     const float adtm = -kappa * (tv * x5b + tvdev * (al * dv0 + w3 * sdv) +
                                  tvb * (V(LBM_VERT_WP, k) * pa + w3 * spv));
     const float hadv = t0 * divb + tdev * dv0;
-    const float vadvT = vadv_p(tm_, t0, tp, sb0, sb1, hasm, hasp, dsk) +
-                        vadv_b(tb, htm, htp, sd0, sd1, hasm, hasp, dsk);
-    float* go = g9 + (size_t)(2 + k * 9) * I;
-    go[0 * I] = adtm + hadv + vadvT;                                  // gt
+    go[0 * I] = adtm + hadv + vp_(tm_, t0, tp) + vb_(tb, htm, htp);  // gt
     go[1 * I] = u0 * tdev + ub * t0;                                  // xu
     const float rcpg = V(LBM_VERT_RCPG, k);
-    float fu = v0 * absv + vb * vo0 - rcpg * (tv * pixb + tvdev * pix);
-    float fv = -u0 * absv - ub * vo0 - rcpg * (tv * piyb + tvdev * piy);
-    fu += vadv_p(um, u0, up, sb0, sb1, hasm, hasp, dsk) +
-          vadv_b(ub, hum, hup, sd0, sd1, hasm, hasp, dsk);
-    fv += vadv_p(vm, v0, vp, sb0, sb1, hasm, hasp, dsk) +
-          vadv_b(vb, hvm, hvp, sd0, sd1, hasm, hasp, dsk);
+    const float fu = v0 * absv + vb * vo0 - rcpg * (tv * pixb + tvdev * pix) +
+                     vp_(um, u0, up) + vb_(ub, hum, hup);
+    const float fv = -u0 * absv - ub * vo0 - rcpg * (tv * piyb + tvdev * piy) +
+                     vp_(vm, v0, vp) + vb_(vb, hvm, hvp);
     go[4 * I] = fu;
     go[5 * I] = fv;
     float ke = phiv + u0 * ub + v0 * vb;
     if (!d.strictly_linear) ke += 0.5f * (u0 * u0 + v0 * v0);
     go[6 * I] = ke;
     go[7 * I] = v0 * tdev + vb * t0;                                  // xv
-    go[2 * I] = q0 * divb + qb * dv0 +                                // g
-                vadv_p(qm, q0, qp, sb0, sb1, hasm, hasp, dsk) +
-                vadv_b(qb, hqm, hqp, sd0, sd1, hasm, hasp, dsk);
+    go[2 * I] = q0 * divb + qb * dv0 + vp_(qm, q0, qp) + vb_(qb, hqm, hqp);   // g
     go[3 * I] = u0 * qb + ub * q0;                                    // yu
     go[8 * I] = v0 * qb + vb * q0;                                    // yv
     // advance the window
@@ -288,6 +288,10 @@ __global__ void __launch_bounds__(I) k_alg(SD<float> d, int ps_mode) {
     hum = hup; hvm = hvp; htm = htp; hqm = hqp;
     sdlo = sdup;
     sb0 = sb1;
+    bk += I;
+    bsk += I;
+    gl += SF_N * I;
+    go += 9 * I;
   }
 }
 
