@@ -1,5 +1,5 @@
 // FP32 grid-point step split into three kernels with full-size work per
-// launch (included by stepper.cu after grid_dft.cuh):
+// launch (included by stepper.cu):
 //
 //   k_idft  per (latitude, member): the longitude synthesis of the six
 //           surface rows and the 6 K level rows of sf/sfs -> grid6
@@ -14,7 +14,9 @@
 //   k_fdft  per (latitude, member): the weighted longitude analysis of grid9
 //           -> af/afs.
 //
-// The DFTs use the quarter-wave folding of grid_dft.cuh.
+// The longitude transforms are dense DFTs folded by quarter-wave symmetry:
+// the points i, I - i, I/2 - i, I/2 + i share |cos| and |sin| of every
+// wavenumber, so even and odd m are accumulated apart over i <= I/4.
 
 namespace lbm {
 
@@ -247,8 +249,13 @@ __global__ void __launch_bounds__(I) k_alg(SD<float> d, int ps_mode) {
     pref3 += V(LBM_VERT_RDLOG3, k) * xv;
     const float sdv = dh - prefd, spv = sx - prefp;                   // suffix sums above k
     const float sd0 = hasm ? sdlo : 0.f, sd1 = hasp ? sdup : 0.f;
-    // vertical advection in differences (vadv_p / vadv_b) times 1 / dsig_k:
-    // perturbation fields by the basic sigma-dot, basic fields by sigma-dot'
+    // vertical advection of dynamics.py's _vert_advect written in differences,
+    //   (s1 (f[k+1] - f[k]) / 2 + s0 (f[k] - f[k-1]) / 2) / dsig_k
+    // (at the bottom / top the missing half becomes +s0 f[k] / -s1 f[k]),
+    // equal to the flux form (F[k+1/2] - F[k-1/2] - f[k] (s1 - s0)) / dsig_k
+    // without cancelling the f[k] (s1 - s0) part: perturbation fields by the
+    // basic sigma-dot, basic fields (half differences precomputed in FP64)
+    // by sigma-dot'
     auto vp_ = [&](float fm, float f0, float fp) {
       const float a = hasp ? 0.5f * sb1 * (fp - f0) : -sb1 * f0;
       const float b = hasm ? 0.5f * sb0 * (f0 - fm) : sb0 * f0;

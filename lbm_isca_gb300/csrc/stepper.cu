@@ -25,6 +25,7 @@
 // no second pass over the levels.
 #include "lbm_common.cuh"
 #include "lbm_fft.cuh"
+#include "async_copy.cuh"
 #include <cmath>
 #include <mutex>
 #include <new>
@@ -361,22 +362,6 @@ template <typename R> struct PairRows {
   LBM_D int n_of(int r) const { return r < L1 ? m1 + r : m2 + (r - L1); }
 };
 
-// Asynchronous global -> shared copy of 16 bytes (cp.async).
-LBM_D void cp_async_16b(void* smem, const void* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-// Asynchronous global -> shared copy of one complex value (cp.async).
-template <typename R> LBM_D void cp_async_c2(C2<R>* smem, const C2<R>* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  if constexpr (sizeof(C2<R>) == 16)
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-LBM_D void cp_async_commit_group() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-LBM_D void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
-
 template <typename R, int NC, int KC>
 __global__ void k_anal(SD<R> d) {
   const int p = blockIdx.x, e = blockIdx.y, kc = blockIdx.z;
@@ -434,18 +419,18 @@ __global__ void k_anal(SD<R> d) {
       const int jn = jh0 + jj, j = hemi ? J - 1 - jn : jn;
       C2<R>* dst = rb + (size_t)((mm * AN_JC + jj) * 2 + hemi) * rowst + c;
       const C2<R>* src = afe + (((size_t)m * J + j) * K + k0) * AF_N + c;
-      if (wide) cp_async_16b(dst, src);
+      if (wide) cp_async16(dst, src);
       else cp_async_c2(dst, src);
     }
-    cp_async_commit_group();
+    cp_async_commit();
   };
   prefetch(0, 0);
   int buf = 0;
   for (int jh0 = 0; jh0 < JH; jh0 += AN_JC) {
     const int jc = min(AN_JC, JH - jh0);
     if (jh0 + AN_JC < JH) prefetch(jh0 + AN_JC, buf ^ 1);
-    else cp_async_commit_group();
-    cp_async_wait_one();
+    else cp_async_commit();
+    cp_async_wait<1>();
     __syncthreads();
     if (active) {
       const C2<R>* rb = raw + buf * rawbuf;
@@ -935,7 +920,6 @@ __global__ void k_ps_flush(SD<R> d, int ps_mode) {
 }
 
 }  // namespace lbm
-#include "grid_dft.cuh"
 #include "grid_split.cuh"
 namespace lbm {
 
