@@ -614,8 +614,9 @@ __global__ void __launch_bounds__(IM_THREADS) k_implicit(SD<R> d, R dt, int set,
     if (act) A[k] = bT + (bT * ktt + wT) * dt;
     __syncthreads();
     if (act) {
-      CX<R> phi = cx_prod(vs[0 * K + k], A[k]);            // WW wdx
-      for (int l = 0; l < k; ++l) phi = cx_add(phi, cx_prod(vs[1 * K + l], A[l]));
+      C2<R> pre = z;                                       // sum_{l<k} R dlog3_l wdx_l
+      for (int l = 0; l < k; ++l) cfma(pre, vs[1 * K + l], A[l]);
+      CX<R> phi = cx_add(cx_prod(vs[0 * K + k], A[k]), cx(pre));   // WW wdx
       const C2<R> wdpix = pp + wpi * dt;
       const R gk = vs[2 * K + k];
       // wdphiy = WW wdx + ft gg wdpix, ft gg taken as gg + bt gg
@@ -636,8 +637,9 @@ __global__ void __launch_bounds__(IM_THREADS) k_implicit(SD<R> d, R dt, int set,
     __syncthreads();
     C2<R> nV = z, nD = z, nT = z, nQ = z, npi = z;
     if (act) {
-      CX<R> sfx = cx<R>(z);                                 // sum_{l>k} dsig_l dbar_l
-      for (int l = K - 1; l > k; --l) sfx = cx_add(sfx, cx_prod(vs[3 * K + l], A[l]));
+      C2<R> suf = z;                                        // sum_{l>k} dsig_l dbar_l
+      for (int l = K - 1; l > k; --l) cfma(suf, vs[3 * K + l], A[l]);
+      const CX<R> sfx = cx(suf);
       const CX<R> corr = cx_mul(cx_add(cx_prod(vs[4 * K + k], dbar), cx_mul(sfx, vs[5 * K + k])),
                                 ktr[k]);
       const C2<R> yT = bT + cx_val(cx_add(cx(wT), cx_neg(corr))) * dt2;
@@ -693,17 +695,17 @@ __global__ void __launch_bounds__(IM_THREADS) k_implicit(SD<R> d, R dt, int set,
     if (act) { A[k] = nV; B[k] = nD; }
     __syncthreads();
     if (act && k == 0) {
-      CX<R> sv = cx<R>(z), sdv = cx<R>(z);
+      C2<R> sv = z, sdv = z;
       for (int l = 0; l < K; ++l) {
-        sv = cx_add(sv, cx_prod(vs[3 * K + l], A[l]));
-        sdv = cx_add(sdv, cx_prod(vs[3 * K + l], B[l]));
+        cfma(sv, vs[3 * K + l], A[l]);
+        cfma(sdv, vs[3 * K + l], B[l]);
       }
       const R il = d.invlap[n];
       const size_t es = (size_t)e * 4 * NS;
       d.sas[es + 0 * NS + idx] = npi;
-      d.sas[es + 1 * NS + idx] = cx_val(cx_mul(sv, il));     // sum dsig psi
-      d.sas[es + 2 * NS + idx] = cx_val(cx_mul(sdv, il));    // sum dsig chi
-      d.sas[es + 3 * NS + idx] = cx_val(sdv);                // sum dsig div
+      d.sas[es + 1 * NS + idx] = sv * il;     // sum dsig psi
+      d.sas[es + 2 * NS + idx] = sdv * il;    // sum dsig chi
+      d.sas[es + 3 * NS + idx] = sdv;         // sum dsig div
     }
   }
 }
