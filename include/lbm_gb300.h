@@ -279,6 +279,18 @@ int lbm_graph_capture(const lbm_stepper_desc* d, const lbm_step_ctl* ctl,
 int lbm_graph_launch(lbm_graph* g, void* stream);
 int lbm_graph_destroy(lbm_graph* g);
 
+/* Daily history accumulation (model.py:257-277).  The reference writes, per
+ * output day, the mean of the trapezoid 0.5 (top(s) + top(s-1)) of its
+ * top-of-step diagnostics (psi, chi, u, v, omega, T, z, ps).  All eight are
+ * linear in the spectral state and the grid ps', so the stepper accumulates
+ * those with the same weights and forms the fields once per day from the
+ * mean.  Elementwise over n reals of precision `prec` (a complex value is two):
+ *   mode 0: prev = cur                          (start-up step: no sample)
+ *   mode 1: acc += w (cur + prev); prev = cur   (w = 1/2 for the trapezoid)
+ * acc is FP64 [n]; cur and prev are (R)[n]. */
+int lbm_history_accumulate(int prec, int64_t n, const void* cur, void* prev,
+                           double* acc, double w, int mode, void* stream);
+
 /* ---- Stepping without allocating -------------------------------------------
  * No counterpart in the reference, whose step functions allocate their work
  * arrays through the array backend on every call.

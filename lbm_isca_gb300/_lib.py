@@ -89,6 +89,7 @@ _SIGS = {
     "lbm_graph_launch": (I32, [VP, VP]),
     "lbm_graph_destroy": (I32, [VP]),
     "lbm_stepper_run_noalloc": (I32, [C.POINTER(StepperDesc), C.POINTER(StepCtl), I32, VP]),
+    "lbm_history_accumulate": (I32, [I32, C.c_int64, VP, VP, VP, F64, I32, VP]),
 }
 
 _LIB = None

@@ -25,6 +25,8 @@ from __future__ import annotations
 import time as _time
 from dataclasses import dataclass, field
 
+import types
+
 import numpy as np
 import torch
 
@@ -201,8 +203,11 @@ class LBM:
         if verbose:
             print(f"  backend: {self.device}", flush=True)
         sched = self._schedule(nsteps)
-        if writer is None and cfg.fused:
-            self._run_fused(sched, mjo_forcing, steady_forcing, verbose, progress_every, t0)
+        nonzero = any(bool((getattr(st, k) != 0).any()) for st in (self.ga, self.gb)
+                      for k in ("u", "v", "t", "q", "ps"))
+        if cfg.fused and (writer is None or not nonzero):
+            self._run_fused(sched, mjo_forcing, steady_forcing, verbose, progress_every, t0,
+                            writer=writer)
         else:
             self._run_general(sched, mjo_forcing, steady_forcing, writer, verbose,
                               progress_every, t0)
@@ -310,7 +315,29 @@ class LBM:
         s = sp._anal(sp._fwd(g4), sp._t["Pgw"], 0)
         return s if is3d else s[..., 0]
 
-    def _run_fused(self, sched, mjo_forcing, sf, verbose, progress_every, t0):
+    def _diagnostics_mean(self, spec, ps):
+        """The eight history fields of a mean spectral state and mean grid ps'
+        (the reference's diagnostics, model.py:151-166, are linear in both, so
+        this equals the mean of the per-step fields)."""
+        sp, vg = self.sp, self.vg
+        if not self.batched:
+            spec = {k: v[0] for k, v in spec.items()}
+            ps = ps[0]
+        u, v = sp.vordiv_to_uv(spec["vor"], spec["div"])
+        t = sp.wave_to_grid(spec["t"])
+        q = sp.wave_to_grid(spec["q"])
+        vor = sp.wave_to_grid(spec["vor"])
+        div = sp.wave_to_grid(spec["div"])
+        pix, piy = sp.hgrad(spec["pi"])
+        st = types.SimpleNamespace(u=u, v=v, t=t, q=q, ps=ps)
+        o = self.dyn._grid_kernel(st, vor, div, pix, piy, None, None, None)
+        psi = sp.wave_to_grid(sp.inverse_laplacian(spec["vor"]))
+        chi = sp.wave_to_grid(sp.inverse_laplacian(spec["div"]))
+        z = vg.hydrostatic(t) / GRAV
+        return {"psi": psi, "chi": chi, "u": u, "v": v, "w": o["omega"], "t": t, "z": z,
+                "p": ps}
+
+    def _run_fused(self, sched, mjo_forcing, sf, verbose, progress_every, t0, writer=None):
         cfg = self.cfg
         stp = self.stepper()
         stp.set_timesteps(sorted({dt for dt, _ in sched}))
@@ -346,8 +373,47 @@ class LBM:
             return
         self._load_stepper(stp)
         spd = cfg.steps_per_day
+        out_every = int(round(cfg.out_interval_days * spd))
+        day_done, sampled = 0, False
+        if writer is not None:
+            stp.hist_begin()
         i = first
         while i < len(sched):
+            if writer is not None:
+                # history: one step per call, sampled around its kernels
+                dt, start = sched[i]
+                if mjo_forcing is not None:
+                    src = mjo_forcing.step()
+                    if src is not last_src[0]:
+                        last_src[0] = src
+                        install(self._spec_forcing(src, True))
+                mode = 0 if start else 1
+                if i == len(sched) - 1:
+                    self._last_top = stp.snapshot()
+                if mode == 1 and not sampled:
+                    stp.hist_sample("spec", 0)           # no earlier top: prev = cur
+                if mode == 1 and not cfg.time_average:
+                    stp.hist_reset()
+                stp.hist_sample("spec", mode)
+                stp.run([(dt, start)], use_graph=False)
+                if mode == 1 and not sampled:
+                    stp.hist_sample("ps", 0)
+                stp.hist_sample("ps", mode)
+                sampled = True
+                i += 1
+                if not start:
+                    self.time += dt
+                    advanced += 1
+                    if advanced % out_every == 0:
+                        day_done += 1
+                        fields = self._diagnostics_mean(*stp.hist_mean())
+                        writer.add(day_done, {k: asnumpy(v) for k, v in fields.items()})
+                        stp.hist_reset()
+                    if advanced % spd == 0 and not stp.check_finite():
+                        raise FloatingPointError(
+                            f"model blew up at or before step {i} of this run "
+                            f"(t={self.time / 86400:.2f} d)")
+                continue
             if mjo_forcing is not None:
                 # time-varying forcing: one .step() call per model step
                 src = mjo_forcing.step()

@@ -323,6 +323,52 @@ class EnsembleStepper:
                                           stream_handle(self.stream)), "lbm_stepper_flush")
         self.pending_ps_mode = 0
 
+    # ---- daily history (model.py:257-277) ---------------------------------
+    def hist_begin(self):
+        """FP64 accumulators and previous-sample copies of the spectral state
+        (sa3, sas) and the grid ps' (psa) for the daily history means."""
+        self._hist = {}
+        for name in ("sa3", "sas", "psa"):
+            cur = getattr(self, name)
+            n = cur.numel() * (2 if cur.is_complex() else 1)
+            self._hist[name] = (torch.zeros_like(cur),
+                                torch.zeros(n, device=self.dev, dtype=torch.float64))
+        self.hist_n = 0
+
+    def hist_sample(self, what, mode):
+        """Accumulate the top-of-step sample: what = "spec" (state, before the
+        step's kernels) or "ps" (grid ps', after them); mode 0 only records
+        the sample (start-up steps), mode 1 adds 0.5 (cur + previous)."""
+        names = ("sa3", "sas") if what == "spec" else ("psa",)
+        for name in names:
+            cur = getattr(self, name)
+            prev, acc = self._hist[name]
+            check(lib().lbm_history_accumulate(self.prec_id, acc.numel(), ptr(cur), ptr(prev),
+                                               ptr(acc), 0.5, mode, stream_handle(self.stream)),
+                  "lbm_history_accumulate")
+        if what == "ps" and mode == 1:
+            self.hist_n += 1
+
+    def hist_reset(self):
+        self.stream.wait_stream(torch.cuda.default_stream(self.dev))
+        with torch.cuda.stream(self.stream):
+            for _, acc in self._hist.values():
+                acc.zero_()
+        self.hist_n = 0
+
+    def hist_mean(self):
+        """Mean spectral state (rectangle complex128 dict incl. pi, member axis
+        first) and mean grid ps' [E][J][I] of the accumulated samples."""
+        torch.cuda.default_stream(self.dev).wait_stream(self.stream)
+        n = max(self.hist_n, 1)
+        E, NS, K = self.E, self.NS, self.K
+        a3 = torch.view_as_complex(self._hist["sa3"][1].view(E, 4, NS, K, 2)) / n
+        as_ = torch.view_as_complex(self._hist["sas"][1].view(E, 4, NS, 2)) / n
+        spec = {k: self.unpack(a3[:, i]) for i, k in enumerate(("vor", "div", "t", "q"))}
+        spec["pi"] = self.unpack(as_[:, 0], has_k=False)
+        ps = self._hist["psa"][1].view(E, self.J, self.I) / n
+        return spec, ps
+
     def check_finite(self):
         self.stream.synchronize()
         return int(self.err.item()) == 0

@@ -285,3 +285,42 @@ def test_fp32_ensemble_within_1e5_of_fp64_at_day10():
         r, f = out["fp64"][k], out["fp32"][k]
         e = float(torch.linalg.norm(f - r) / torch.linalg.norm(r))
         assert e <= 1e-5, (k, e)
+
+
+class _Writer:
+    """Collects the history records the model writes (output.py's protocol)."""
+
+    def __init__(self):
+        self.days = []
+        self.closed = False
+
+    def add(self, day, fields):
+        self.days.append((day, {k: np.array(v) for k, v in fields.items()}))
+
+    def close(self):
+        self.closed = True
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32", 2e-5)])
+def test_fused_history_matches_general_loop(precision, tol):
+    """Daily trapezoid-mean history (model.py:257-277) accumulated on the
+    device by the fused stepper equals the general loop's per-step average."""
+    from lbm_isca_gb300 import LBM, Config, VerticalGrid
+    sp = _t21()
+    sigm = configs.equal_sigma_half_levels(20)
+    vg = VerticalGrid(sigm=sigm, device="gb300")
+    bs = configs.solid_body_basic_state(64, 32, sigm)
+    heat = configs.elliptic_heating(64, 32, sigm)
+    out = {}
+    for fused, prec in ((False, "fp64"), (True, precision)):
+        cfg = Config(ndays=2.0, fused=fused, precision=prec, **configs.plain_damping(20))
+        w = _Writer()
+        LBM(bs, sp, vg, cfg).run(steady_forcing=_Steady(heat, 32, 64, 20), writer=w,
+                                 verbose=False)
+        assert w.closed and [d for d, _ in w.days] == [1, 2]
+        out[fused] = w.days
+    for (_, ref), (_, got) in zip(out[False], out[True]):
+        assert set(ref) == {"psi", "chi", "u", "v", "w", "t", "z", "p"}
+        for k in ref:
+            e = np.linalg.norm(got[k] - ref[k]) / np.linalg.norm(ref[k])
+            assert e < tol, (k, e)
