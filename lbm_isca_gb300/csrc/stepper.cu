@@ -935,9 +935,34 @@ template <typename R, int I> constexpr int grid_nt() {
   return I == 64 ? 128 : ((I == 256 && sizeof(R) == 8) ? 128 : 256);
 }
 
-template <typename R> size_t anal_smem(int NR, int JH) {
+template <typename R> size_t anal_smem(int NR, int JH, int KC) {
   return sizeof(R) * 2 * (size_t)NR * JH + 16 +
-         sizeof(C2<R>) * (size_t)2 * (2 * AN_JC * 2 * AF_N * Cfg<R>::KCA);
+         sizeof(C2<R>) * (size_t)2 * (2 * AN_JC * 2 * AF_N * KC);
+}
+// Level chunk of the analysis block (one thread per level and row group): the
+// preferred Cfg<R>::KCA, halved where that block would exceed 256 threads.
+template <typename R> int anal_kc(int N) {
+  constexpr int NC = Cfg<R>::NC;
+  const int G = (N + 2 + NC - 1) / NC + 1;
+  return (Cfg<R>::KCA * G > 256) ? Cfg<R>::KCA / 2 : Cfg<R>::KCA;
+}
+template <typename R, int KC> void launch_anal(const SD<R>& d, cudaStream_t st, bool attrs) {
+  constexpr int NC = Cfg<R>::NC;
+  const int JH = d.J / 2, NRmax = d.N + 2, NP = (d.M + 1) / 2;
+  const int G = (d.N + 2 + NC - 1) / NC + 1;
+  const int nt = ((KC * G + 31) / 32) * 32;
+  // the surface pass also needs 2 * JH * 2 staging elements
+  size_t sm = anal_smem<R>(NRmax, JH, KC);
+  const size_t sm2 = sizeof(R) * 2 * (size_t)NRmax * JH + 16 + sizeof(C2<R>) * (size_t)2 * JH * 2 * 2;
+  if (sm2 > sm) sm = sm2;
+  if (attrs)
+    cudaFuncSetAttribute(k_anal<R, NC, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  else
+    k_anal<R, NC, KC><<<dim3(NP, d.E, (d.K + KC - 1) / KC), nt, sm, st>>>(d);
+}
+template <typename R> void run_anal(const SD<R>& d, cudaStream_t st, bool attrs) {
+  if (anal_kc<R>(d.N) == Cfg<R>::KCA) launch_anal<R, Cfg<R>::KCA>(d, st, attrs);
+  else launch_anal<R, Cfg<R>::KCA / 2>(d, st, attrs);
 }
 template <typename R> size_t synth_smem(int NR, int JH) {
   return sizeof(R) * 2 * (size_t)NR * JH + sizeof(C2<R>) * (size_t)NR * Cfg<R>::KCS * 6;
@@ -970,16 +995,7 @@ template <typename R, int I> int launch_step(const SD<R>& d, const lbm_step_ctl&
     if (only < 0 || only == 0)
       k_grid<R, I, KB, NT><<<dim3(d.J, d.E), NT, gsm, st>>>(d, c.ps_mode);
   }
-  if (only < 0 || only == 1) {
-    constexpr int NC = Cfg<R>::NC, KC = Cfg<R>::KCA;
-    const int G = (d.N + 2 + NC - 1) / NC + 1;
-    const int nt = ((KC * G + 31) / 32) * 32;
-    // the surface pass also needs 2 * JH * 2 staging elements
-    size_t sm = anal_smem<R>(NRmax, JH);
-    const size_t sm2 = sizeof(R) * 2 * (size_t)NRmax * JH + 16 + sizeof(C2<R>) * (size_t)2 * JH * 2 * 2;
-    if (sm2 > sm) sm = sm2;
-    k_anal<R, NC, KC><<<dim3(NP, d.E, (d.K + KC - 1) / KC), nt, sm, st>>>(d);
-  }
+  if (only < 0 || only == 1) run_anal<R>(d, st, false);
   if (only < 0 || only == 2)
     k_implicit<R><<<dim3(NP, d.E), IM_THREADS, impl_smem<R>(d.K), st>>>(d, R(c.dt), c.set,
                                                                          c.ra_mode);
@@ -1006,11 +1022,7 @@ template <typename R, int I> void set_attrs(const SD<R>& d) {
     cudaFuncSetAttribute(k_grid<R, I, KB, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)GridSmem<R, I, KB, NT>::bytes(d.M));
   }
-  size_t sm = anal_smem<R>(NRmax, JH);
-  const size_t sm2 = sizeof(R) * 2 * (size_t)NRmax * JH + 16 + sizeof(C2<R>) * (size_t)2 * JH * 2 * 2;
-  if (sm2 > sm) sm = sm2;
-  cudaFuncSetAttribute(k_anal<R, Cfg<R>::NC, Cfg<R>::KCA>,
-                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  run_anal<R>(d, nullptr, true);
   cudaFuncSetAttribute(k_implicit<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)impl_smem<R>(d.K));
   cudaFuncSetAttribute(k_synth<R, Cfg<R>::JG, Cfg<R>::KCS>,
@@ -1071,6 +1083,19 @@ template <typename R> int prepare_attrs(const lbm_stepper_desc* desc) {
   const SD<R> d = make_sd<R>(*desc);
   int rc = validate(d);
   if (rc) return rc;
+  {
+    // the analysis block holds one thread per (level, row group) of an m-pair
+    constexpr int NC = Cfg<R>::NC;
+    const int KC = anal_kc<R>(d.N);
+    const int G = (d.N + 2 + NC - 1) / NC + 1;
+    const int nt = ((KC * G + 31) / 32) * 32;
+    cudaFuncAttributes fa;
+    const cudaError_t ea = (KC == Cfg<R>::KCA)
+                               ? cudaFuncGetAttributes(&fa, k_anal<R, NC, Cfg<R>::KCA>)
+                               : cudaFuncGetAttributes(&fa, k_anal<R, NC, Cfg<R>::KCA / 2>);
+    if (ea != cudaSuccess) return LBM_ERR_LAUNCH;
+    if (nt > fa.maxThreadsPerBlock) return LBM_ERR_ARG;
+  }
   switch (d.I) {
     case 64: set_attrs<R, 64>(d); break;
     case 128: set_attrs<R, 128>(d); break;

@@ -324,3 +324,35 @@ def test_fused_history_matches_general_loop(precision, tol):
         for k in ref:
             e = np.linalg.norm(got[k] - ref[k]) / np.linalg.norm(ref[k])
             assert e < tol, (k, e)
+
+
+def _t85l40_model(fused, precision, ndays):
+    from lbm_isca_gb300 import LBM, Config, Spectral, VerticalGrid
+    sp = Spectral(nlon=256, nlat=128, nmax=85, device="gb300")
+    sigm = configs.equal_sigma_half_levels(40)
+    vg = VerticalGrid(sigm=sigm, device="gb300")
+    bs = configs.solid_body_basic_state(256, 128, sigm)
+    cfg = Config(ndays=ndays, fused=fused, precision=precision, **configs.plain_damping(40))
+    return LBM(bs, sp, vg, cfg), sigm
+
+
+def test_t85l40_fused_matches_general_loop():
+    """The largest configuration (T85L40, 256x128 grid): the fused FP64
+    stepper against the reference step sequence (general loop) over 6 steps,
+    and the FP32 stepper against FP64 over 4 model hours."""
+    ndays = 6 / 72.0
+    res = {}
+    for fused, prec in ((False, "fp64"), (True, "fp64")):
+        m, sigm = _t85l40_model(fused, prec, ndays)
+        heat = configs.elliptic_heating(256, 128, sigm)
+        m.run(steady_forcing=_Steady(heat, 128, 256, 40), verbose=False)
+        res[(fused, prec)] = m.ga
+    for k in ("u", "v", "t", "ps"):
+        r, g = _np(getattr(res[(False, "fp64")], k)), _np(getattr(res[(True, "fp64")], k))
+        assert relerr(g, r) < 1e-10, k
+    m, sigm = _t85l40_model(True, "fp32", ndays)
+    heat = configs.elliptic_heating(256, 128, sigm)
+    m.run(steady_forcing=_Steady(heat, 128, 256, 40), verbose=False)
+    for k in ("u", "v", "t", "ps"):
+        r, g = _np(getattr(res[(True, "fp64")], k)), _np(getattr(m.ga, k))
+        assert relerr(g, r) < 1e-5, k
