@@ -630,7 +630,11 @@ __global__ void __launch_bounds__(IM_THREADS) k_implicit(SD<R> d, R dt, int set,
     C2<R> dbar = z;
     if (act) {
       const R* mm_ = mi + sel * K * K;
-      for (int l = 0; l < K; ++l) cfma(dbar, mm_[l * K + k], B[l]);   // minv stored (l, k)
+      // M(n)^-1 rhs with exact products and compensated sums (the divergence
+      // of a balanced flow is small against the terms of this sum)
+      CX<R> acc = cx<R>(z);
+      for (int l = 0; l < K; ++l) acc = cx_add(acc, cx_prod(mm_[l * K + k], B[l]));   // minv (l, k)
+      dbar = cx_val(acc);
     }
     __syncthreads();
     if (act) A[k] = dbar;
