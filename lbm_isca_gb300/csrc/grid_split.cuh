@@ -55,13 +55,13 @@ __global__ void __launch_bounds__(SPLIT_NT) k_idft(SD<float> d, const float2* __
   // rows v0 .. v0 + RC - 1 of chunk into buffer b: level rows by cp.async (16
   // bytes = two rows of one m), the surface rows (chunk 0) by plain loads
   auto stage = [&](int v0, int b) {
-    float2* F = fin + (size_t)b * M * RC;
+    float2* F = fin + b * M * RC;
     const int vs = max(v0, 6), ve = min(v0 + RC, NR);
     if (ve > vs) {
       const int half = (ve - vs) >> 1;           // (ve - vs) and (vs - 6) are even
       for (int x = tid; x < M * half; x += NT) {
         const int m = x / half, c = 2 * (x - m * half);
-        cp_async16(F + (size_t)m * RC + (vs - v0) + c,
+        cp_async16(F + m * RC + (vs - v0) + c,
                    sfe + ((size_t)m * J + j) * K * SF_N + (vs - 6) + c);
       }
     }
@@ -71,11 +71,11 @@ __global__ void __launch_bounds__(SPLIT_NT) k_idft(SD<float> d, const float2* __
         const int m = x / SFS_N, f = x - m * SFS_N;
         const float2 X = sfs[(((size_t)e * M + m) * J + j) * SFS_N + f];
         if (f == SFS_PI) {
-          F[(size_t)m * RC + 0] = X;
-          F[(size_t)m * RC + 1] = make_float2(-X.y * m * rcos, X.x * m * rcos);
+          F[m * RC + 0] = X;
+          F[m * RC + 1] = make_float2(-X.y * m * rcos, X.x * m * rcos);
         } else {
           const float s = (f == SFS_DH) ? 1.f : rcos;
-          F[(size_t)m * RC + f + 1] = make_float2(X.x * s, X.y * s);
+          F[m * RC + f + 1] = make_float2(X.x * s, X.y * s);
         }
       }
     }
@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(SPLIT_NT) k_idft(SD<float> d, const float2* __
     else cp_async_commit();
     cp_async_wait<1>();
     __syncthreads();
-    const float2* F = fin + (size_t)buf * M * RC;
+    const float2* F = fin + buf * M * RC;
     // points i = 1..Q, RG rows per item: x_i, x_{I-i}, x_{I/2-i}, x_{I/2+i}
     constexpr int NGR = RC / RG;
     for (int it = tid; it < Q * NGR; it += NT) {
@@ -109,8 +109,8 @@ __global__ void __launch_bounds__(SPLIT_NT) k_idft(SD<float> d, const float2* __
       int m = 1;
       for (; m + 1 < M; m += 2) {              // (odd, even) pairs of m >= 1
         const float2 to = tb[m * (Q + 1)], te = tb[(m + 1) * (Q + 1)];
-        const float4* xo = reinterpret_cast<const float4*>(F + (size_t)m * RC + r0);
-        const float4* xe = reinterpret_cast<const float4*>(F + (size_t)(m + 1) * RC + r0);
+        const float4* xo = reinterpret_cast<const float4*>(F + m * RC + r0);
+        const float4* xe = reinterpret_cast<const float4*>(F + (m + 1) * RC + r0);
 #pragma unroll
         for (int t = 0; t < RG / 2; ++t) {
           const float4 b = xo[t], a = xe[t];
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(SPLIT_NT) k_idft(SD<float> d, const float2* __
       }
       if (m < M) {                              // last (odd) m
         const float2 to = tb[m * (Q + 1)];
-        const float4* xo = reinterpret_cast<const float4*>(F + (size_t)m * RC + r0);
+        const float4* xo = reinterpret_cast<const float4*>(F + m * RC + r0);
 #pragma unroll
         for (int t = 0; t < RG / 2; ++t) {
           const float4 b = xo[t];
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(SPLIT_NT) k_idft(SD<float> d, const float2* __
     for (int r = tid; r < nr; r += NT) {
       float se_ = 0.f, so_ = 0.f;
       for (int m = 1; m < M; ++m) {
-        const float a = F[(size_t)m * RC + r].x;
+        const float a = F[m * RC + r].x;
         if (m & 1) so_ += a;
         else se_ += a;
       }
@@ -384,7 +384,7 @@ __global__ void __launch_bounds__(SPLIT_NT) k_fdft(SD<float> d, const float2* __
     __syncthreads();
     for (int x = tid; x < nrow * (Q + 1); x += NT) {
       const int r = x / (Q + 1), i = x - r * (Q + 1);
-      const float* row = raw + (size_t)r * I;
+      const float* row = raw + r * I;
       float4 v;
       if (i == 0) {
         const float xq = row[Q], x3q = row[3 * Q];
@@ -418,11 +418,11 @@ __global__ void __launch_bounds__(SPLIT_NT) k_fdft(SD<float> d, const float2* __
       }
       const float4* w[4];
 #pragma unroll
-      for (int t = 0; t < 4; ++t) w[t] = fw + (size_t)(rw[t] >= 0 ? rw[t] : 0) * (Q + 1);
+      for (int t = 0; t < 4; ++t) w[t] = fw + (rw[t] >= 0 ? rw[t] : 0) * (Q + 1);
       float acc[4][4];
 #pragma unroll
       for (int t = 0; t < 4; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
-      const float4* tb = tab + (size_t)p * (Q + 1);
+      const float4* tb = tab + p * (Q + 1);
 #pragma unroll 4
       for (int i = 1; i < Q; ++i) {
         const float4 c = tb[i];
@@ -452,7 +452,7 @@ __global__ void __launch_bounds__(SPLIT_NT) k_fdft(SD<float> d, const float2* __
         const float2* X = par ? Xo : Xe;
         const float rm = float(m);
         if (q < 2 * lc) {
-          float2* o = fout + (size_t)((q >> 1) * AF_N) * M;
+          float2* o = fout + ((q >> 1) * AF_N) * M;
           if ((q & 1) == 0) {
             // a3 = wg X(gt) - wd i m X(xu); a5 = wg X(g) - wd i m X(yu)
             o[AF_T * M + m] = make_float2(wg * X[0].x + wd * rm * X[1].y,
@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(SPLIT_NT) k_fdft(SD<float> d, const float2* __
         } else if (q < fdft_quads(lc)) {
           for (int t = 0; t < 4; ++t) {
             const int l = 4 * (q - 2 * lc) + t;
-            if (l < lc) fout[(size_t)(l * AF_N + AF_YV) * M + m] = make_float2(wd * X[t].x, wd * X[t].y);
+            if (l < lc) fout[(l * AF_N + AF_YV) * M + m] = make_float2(wd * X[t].x, wd * X[t].y);
           }
         } else {
           float2* o = reinterpret_cast<float2*>(d.afs) + (((size_t)e * M + m) * J + j) * 2;

@@ -417,7 +417,7 @@ __global__ void k_anal(SD<R> d) {
       const int hemi = w & 1, jj = (w >> 1) % jc, mm = (w >> 1) / jc;
       const int m = mm ? pr.m2 : pr.m1;
       const int jn = jh0 + jj, j = hemi ? J - 1 - jn : jn;
-      C2<R>* dst = rb + (size_t)((mm * AN_JC + jj) * 2 + hemi) * rowst + c;
+      C2<R>* dst = rb + ((mm * AN_JC + jj) * 2 + hemi) * rowst + c;
       const C2<R>* src = afe + (((size_t)m * J + j) * K + k0) * AF_N + c;
       if (wide) cp_async16(dst, src);
       else cp_async_c2(dst, src);
@@ -436,7 +436,7 @@ __global__ void k_anal(SD<R> d) {
       const C2<R>* rb = raw + buf * rawbuf;
       for (int jj = 0; jj < jc; ++jj) {
         // north / south rows -> equatorially symmetric [0] and antisymmetric [1] parts
-        const C2<R>* xn = rb + (size_t)((mi * AN_JC + jj) * 2) * rowst + k * AF_N;
+        const C2<R>* xn = rb + ((mi * AN_JC + jj) * 2) * rowst + k * AF_N;
         const C2<R>* xsth = xn + rowst;
         C2<R> x[AF_N][2];
 #pragma unroll
@@ -810,7 +810,7 @@ __global__ void __launch_bounds__(SY_THREADS, 2) k_synth(SD<R> d) {
     // symmetric about the equator (plus), H of an even row antisymmetric.
     auto row = [&](int r, auto par_tag) {
       constexpr int PP = decltype(par_tag)::value, HP = PP ^ 1;
-      const C2<R>* s = sv + (size_t)r * 6 * KC + kk;
+      const C2<R>* s = sv + r * 6 * KC + kk;
       const C2<R> psi = s[0 * KC], chi = s[1 * KC], vo = s[2 * KC], dv = s[3 * KC];
       const C2<R> tt = s[4 * KC], qq = s[5 * KC];
 #pragma unroll
