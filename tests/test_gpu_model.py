@@ -356,3 +356,30 @@ def test_t85l40_fused_matches_general_loop():
     for k in ("u", "v", "t", "ps"):
         r, g = _np(getattr(res[(True, "fp64")], k)), _np(getattr(m.ga, k))
         assert relerr(g, r) < 1e-5, k
+
+
+def test_steady_forcing_all_channels_fused_matches_general():
+    """Steady forcing through every channel the reference accepts (vor, div,
+    T on levels and ps, dynamics.py:189-190, 248-251; forcing.py:71-96): the
+    fused stepper (spectral forcing) against the general loop (grid forcing)
+    over one day at T21L20."""
+    from lbm_isca_gb300 import LBM, Config, VerticalGrid
+    sp = _t21()
+    sigm = configs.equal_sigma_half_levels(20)
+    vg = VerticalGrid(sigm=sigm, device="gb300")
+    bs = configs.solid_body_basic_state(64, 32, sigm)
+    heat = configs.elliptic_heating(64, 32, sigm)
+    lat = np.arcsin(sp.mu)[:, None]
+    lon = sp.lon[None, :]
+    shape2 = np.cos(lat) ** 2 * np.sin(2 * lon)
+    frc = _Steady(heat, 32, 64, 20)
+    frc.vor = 1e-11 * shape2[..., None] * np.ones(20)
+    frc.div = 5e-12 * np.cos(lat)[..., None] * np.cos(lon)[..., None] * np.ones(20)
+    frc.ps = 1e-5 * shape2
+    out = {}
+    for fused in (False, True):
+        m = LBM(bs, sp, vg, Config(ndays=1.0, fused=fused, **configs.plain_damping(20)))
+        m.run(steady_forcing=frc, verbose=False)
+        out[fused] = m.ga
+    for k in ("u", "v", "t", "ps"):
+        assert relerr(_np(getattr(out[True], k)), _np(getattr(out[False], k))) < 1e-10, k
