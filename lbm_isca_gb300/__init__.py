@@ -29,11 +29,12 @@ _LAZY = {
     "device_name": ("backend", "device_name"),
     "asnumpy": ("backend", "asnumpy"),
     "resolve": ("backend", "resolve"),
+    "MJOForcing": ("forcing", "MJOForcing"),
 }
 
 __all__ = ["Spectral", "VerticalGrid", "LBM", "Config", "State", "IMAX", "JMAX", "KMAX",
            "NMAX", "gpu_available", "device_name", "asnumpy", "resolve",
-           "BatchedSpectral", "EnsembleForcing", "make_ensemble_model"]
+           "BatchedSpectral", "EnsembleForcing", "make_ensemble_model", "MJOForcing"]
 
 
 def __getattr__(name):

@@ -33,6 +33,7 @@ import torch
 from .backend import asnumpy, device_name
 from .constants import GRAV
 from .dynamics import BasicStateTerms, Dynamics
+from .forcing import SpectralInterpolation
 from .integrator import Damping, Integrator, SemiImplicit, VerticalDiffusion
 from .state import State
 
@@ -367,6 +368,18 @@ class LBM:
                 self.time += dt
         if mjo_forcing is None:
             install(ft_steady)
+        # a forcing of daily records (MJOForcing): records analysed once, each
+        # step's forcing interpolated in spectral space on the device
+        interp = None
+        if mjo_forcing is not None and SpectralInterpolation.supports(mjo_forcing):
+            interp = SpectralInterpolation(mjo_forcing, lambda g: self._spec_forcing(g, True))
+
+        def next_forcing():
+            src = interp.next() if interp is not None else mjo_forcing.step()
+            if src is not last_src[0]:
+                last_src[0] = src
+                install(src if interp is not None else self._spec_forcing(src, True))
+
         self._last_top = None
         advanced = 1 if (first == 1 and not sched[0][1]) else 0
         if first >= len(sched):
@@ -383,10 +396,7 @@ class LBM:
                 # history: one step per call, sampled around its kernels
                 dt, start = sched[i]
                 if mjo_forcing is not None:
-                    src = mjo_forcing.step()
-                    if src is not last_src[0]:
-                        last_src[0] = src
-                        install(self._spec_forcing(src, True))
+                    next_forcing()
                 mode = 0 if start else 1
                 if i == len(sched) - 1:
                     self._last_top = stp.snapshot()
@@ -416,10 +426,7 @@ class LBM:
                 continue
             if mjo_forcing is not None:
                 # time-varying forcing: one .step() call per model step
-                src = mjo_forcing.step()
-                if src is not last_src[0]:
-                    last_src[0] = src
-                    install(self._spec_forcing(src, True))
+                next_forcing()
                 j = i + 1
             else:
                 j, n_adv = i, 0

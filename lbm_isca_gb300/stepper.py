@@ -176,9 +176,17 @@ class EnsembleStepper:
             fs[:] = p.expand(Ef, self.NS)
         new_ptrs = self.frc3 is None
         if self.frc3 is not None and self.frc3.shape == f3.shape:
-            self.frc3.copy_(f3)
-            self.frcs.copy_(fs)
+            # in place, ordered after the steps already queued on the stepper's
+            # stream (they may still read the old forcing)
+            self.stream.wait_stream(torch.cuda.current_stream(self.dev))
+            with torch.cuda.stream(self.stream):
+                self.frc3.copy_(f3)
+                self.frcs.copy_(fs)
+            f3.record_stream(self.stream)
+            fs.record_stream(self.stream)
         else:
+            # new buffers: the stepper's stream must see them written
+            self.stream.wait_stream(torch.cuda.current_stream(self.dev))
             self.frc3, self.frcs = f3, fs
             new_ptrs = True
         self.frc_shared = 0 if per_member else 1

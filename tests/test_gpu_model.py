@@ -383,3 +383,25 @@ def test_steady_forcing_all_channels_fused_matches_general():
         out[fused] = m.ga
     for k in ("u", "v", "t", "ps"):
         assert relerr(_np(getattr(out[True], k)), _np(getattr(out[False], k))) < 1e-10, k
+
+
+def test_mjo_forcing_spectral_interpolation_matches_general_loop():
+    """Daily-record MJO forcing: the fused stepper's on-device spectral
+    interpolation against the general loop's per-step grid field."""
+    from lbm_isca_gb300 import LBM, Config, VerticalGrid
+    from lbm_isca_gb300.forcing import MJOForcing
+    sp = _t21()
+    sigm = configs.equal_sigma_half_levels(20)
+    vg = VerticalGrid(sigm=sigm, device="gb300")
+    bs = configs.solid_body_basic_state(64, 32, sigm)
+    days = np.stack([configs.elliptic_heating(64, 32, sigm, lon0=lon, lat0=5.0)
+                     for lon in (90.0, 120.0, 150.0)])
+    out = {}
+    for fused in (False, True):
+        f = MJOForcing(days, nt=72, spinup=20)
+        m = LBM(bs, sp, vg, Config(ndays=2.0, fused=fused, **configs.plain_damping(20)))
+        m.run(mjo_forcing=f, verbose=False)
+        out[fused] = m.ga
+        assert f.counter == 2 * 72 + 2
+    for k in ("u", "v", "t", "ps"):
+        assert relerr(_np(getattr(out[True], k)), _np(getattr(out[False], k))) < 1e-10, k

@@ -152,3 +152,25 @@ def test_sharded_members_match_single_process(tmp_path):
     m.run(4, frc_t=heats)
     assert full.shape == m.ga.t.shape
     assert np.abs(full - m.ga.t).max() <= 1e-12 * np.abs(m.ga.t).max()
+
+
+def test_mjo_forcing_call_sequence_and_plan():
+    """MJOForcing follows forcing.py:99-157 (spin-up hold, then linear
+    interpolation over nt calls per day); plan() names the field the next
+    step() returns."""
+    import numpy as np
+    from lbm_isca_gb300.forcing import MJOForcing
+    gtf = np.arange(3)[:, None, None, None] * np.ones((3, 2, 4, 5)) + 1.0
+    f = MJOForcing(gtf, nt=4, spinup=3)
+    for call in range(1, 20):
+        a, b, w = f.plan()
+        got = f.step()
+        want = gtf[a] + (gtf[b] - gtf[a]) * w
+        assert np.allclose(got, want), call
+    # spin-up holds day 1, then day 1 -> day 2 over 4 calls, ...
+    f.reset()
+    vals = [float(f.step()[0, 0, 0]) for _ in range(12)]
+    assert vals[:2] == [1.0, 1.0]
+    assert vals[2:6] == [1.0, 1.25, 1.5, 1.75]
+    assert vals[6:10] == [2.0, 2.25, 2.5, 2.75]
+    assert vals[10:12] == [3.0, 3.0]
