@@ -211,6 +211,7 @@ int lbm_implicit_step(int prec, const lbm_implicit_args* a, void* stream);
  *   frc3 [Ef][4][NS][K], frcs [Ef][NS]: spectral forcing (NULL = none),
  *        Ef = E or 1 (frc_shared = 1)
  *   err [1] int: set nonzero when a non-finite value is produced
+ * sf, af and grid9 must be 16-byte aligned (LBM_ERR_ARG otherwise).
  * ==========================================================================*/
 enum {
   LBM_VERT_DSIG = 0, LBM_VERT_SIGM, LBM_VERT_ALPHA, LBM_VERT_W3, LBM_VERT_WP,

@@ -23,4 +23,10 @@ template <int N> LBM_D void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// Bulk prefetch of `bytes` (a multiple of 16) at `gmem` (16-byte aligned)
+// into L2; no completion is tracked.
+LBM_D void prefetch_l2_bulk(const void* gmem, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(gmem), "r"(bytes) : "memory");
+}
+
 }  // namespace lbm

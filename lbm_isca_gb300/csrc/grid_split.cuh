@@ -303,185 +303,305 @@ __global__ void __launch_bounds__(I) k_alg(SD<float> d, int ps_mode) {
 }
 
 // ---------------------------------------------------------------------------
-// Longitude analysis.  A chunk of LC levels at a time: the 9 LC grid rows
-// (and in the first chunk the two surface rows) stream into shared memory by
-// cp.async while the previous chunk computes, are folded by quarter-wave
-// symmetry into fw[row][i] = (u+uh, u-uh, v-vh, v+vh) (u, v: sum / difference
-// of x_i and x_{I-i}; uh, vh: of x_{I/2-i} and x_{I/2+i}), and each thread
-// item accumulates one "quad" of 4 rows against one wavenumber pair (m even,
-// m odd), reading one packed table entry (cos, sin of the even m, cos, sin of
-// the odd m) per point.
-LBM_HD int fdft_quads(int lc) { return 2 * lc + (lc + 3) / 4; }
-
-struct FdftLayout {
-  int tab, raw, fw, fout, total;     // float units, 16-byte aligned blocks
-  LBM_HD static int al4(int x) { return (x + 3) & ~3; }
-  LBM_HD FdftLayout(int I, int M, int LC) {
-    const int Q = I / 4, NP = (M + 1) / 2, NR = 9 * LC + 2;
-    int o = 0;
-    tab = o; o = al4(o + 4 * NP * (Q + 1));
-    raw = o; o = al4(o + NR * I);
-    fw = o; o = al4(o + 4 * NR * (Q + 1));
-    fout = o; o = al4(o + 2 * LC * AF_N * M);
-    total = o;
-  }
+// Longitude analysis, written as four register-tiled products of folded grid
+// rows with the folded DFT table.
+//
+// Work unit: the rows of LC levels of one (member, latitude) column (the 9 LC
+// level rows gt xu g yu fu fv ke xv yv per level, and in the unit of level 0
+// the two surface rows).  Each row is folded by quarter-wave symmetry into
+// four planes over the points 0 < i < I/4, with u, w the sum / difference of
+// x_i and x_{I-i} and uh, vh those of x_{I/2-i} and x_{I/2+i}:
+//   P0 = u + uh (cos, even m)  P1 = w - vh (sin, even m)
+//   P2 = u - uh (cos, odd m)   P3 = w + vh (sin, odd m)
+// and the table likewise into T0..T3 = cos, sin of m = 2p and of m = 2p + 1.
+// Plane c gives the sums S_c[row][p] = sum_i P_c[i][row] T_c[i][p]; each lane
+// owns one c and an 8-row by 8-pair tile (64 accumulators) and reads per point
+// two float4 of its rows and two of its pairs.  The quarter warps of a half
+// warp hold different planes, so every 16-byte load is one shared-memory
+// wavefront per half warp (conflict-free by the plane and row strides).  The
+// sums go through shared memory to an output pass that combines rows (a3 =
+// wg X(gt) - wd i m X(xu), ...) and writes af/afs with coalesced stores.
+//
+// CTAs are persistent: each walks the units with a grid stride, loads the
+// table once, and streams the next unit's rows into shared memory by
+// cp.async while it computes the current one.
+struct FdftPlan {
+  int lc, nrg, npg, warps, nt;           // levels, row groups, pair groups, warps, threads
+  int rp, ps, npp, ts;                   // strides (floats): plane point, plane, table point,
+                                         //   table plane
+  int tab, pl, b0, total;                // float offsets of the shared-memory blocks, size
 };
 
-// Level chunk: as many levels as keep the thread items of a chunk within one
-// pass of the block and the shared memory within 74 KB (three CTAs on an SM),
-// then evened out over the chunks.
-LBM_HD int fdft_chunk(int I, int M, int K) {
-  const int NP = (M + 1) / 2;
-  int lc = K;
-  while (lc > 1 && ((fdft_quads(lc) + 1) * NP > SPLIT_NT ||
-                    sizeof(float) * (size_t)FdftLayout(I, M, lc).total > 74 * 1024))
-    --lc;
-  const int nchunk = (K + lc - 1) / lc;
-  return (K + nchunk - 1) / nchunk;
+LBM_HD FdftPlan fdft_layout(int I, int M, int lc) {
+  const int Q = I / 4, NP = (M + 1) / 2, nrow = 9 * lc + 2;
+  FdftPlan p;
+  p.lc = lc;
+  p.nrg = (nrow + 7) / 8;
+  p.npg = (NP + 7) / 8;
+  p.warps = (p.nrg * p.npg + 7) / 8;
+  p.nt = 32 * p.warps;
+  p.rp = 8 * p.nrg + 4;                             // = 4 (mod 8): conflict-free fold stores
+  p.ps = Q * p.rp + 4;                              // = 4 (mod 8): planes c, c+1 apart
+  p.npp = 8 * p.npg;
+  p.ts = Q * p.npp + 4;
+  auto al4 = [](int x) { return (x + 3) & ~3; };
+  // the staged outputs [M][7 lc] float2 alias the planes
+  int planes = 4 * p.ps;
+  if (14 * M * lc > planes) planes = 14 * M * lc;
+  int o = 0;
+  p.tab = o; o = al4(o + 4 * p.ts);
+  p.pl = o; o = al4(o + planes);
+  p.b0 = o; o = al4(o + 4 * 8 * p.nrg);
+  p.total = o;
+  return p;
+}
+
+// Levels per unit, evened out over the units of a column: the best product of
+// the useful fraction of the computed rows, the busy fraction of the lanes
+// and the resident warps per SM (shared memory, 128 registers a thread; counted
+// up to 12), more levels on a tie.
+LBM_HD FdftPlan fdft_plan(int I, int M, int K) {
+  float best_score = -1.f;
+  int best = 0;
+  for (int cand = 1; cand <= K; ++cand) {
+    const int nch = (K + cand - 1) / cand, lc = (K + nch - 1) / nch;
+    const FdftPlan p = fdft_layout(I, M, lc);
+    const size_t sm = sizeof(float) * (size_t)p.total;
+    if (p.warps > 8 || sm > 227 * 1024) continue;
+    int ctas = (int)((228 * 1024) / (sm + 1024));
+    const int creg = 65536 / (p.nt * 128);
+    if (creg < ctas) ctas = creg;
+    if (32 / p.warps < ctas) ctas = 32 / p.warps;
+    int w = ctas * p.warps;
+    if (w > 12) w = 12;
+    const float rows = float(9 * lc) / float(8 * p.nrg);
+    const float lanes = float(p.nrg * p.npg) / float(8 * p.warps);
+    const float score = rows * lanes * float(w);
+    if (score >= best_score) { best_score = score; best = lc; }
+  }
+  if (best == 0) {
+    FdftPlan none = fdft_layout(I, M, 1);
+    none.total = 1 << 30;                  // nothing fits: rejected by the caller
+    return none;
+  }
+  return fdft_layout(I, M, best);
 }
 
 template <int I>
-__global__ void __launch_bounds__(SPLIT_NT) k_fdft(SD<float> d, const float2* __restrict__ dft,
-                                                  int LC) {
-  constexpr int Q = I / 4, NT = SPLIT_NT, NW = NT / 32;
-  const int j = blockIdx.x, e = blockIdx.y;
-  const int J = d.J, K = d.K, M = d.M, NP = (M + 1) / 2;
+__global__ void __launch_bounds__(256) k_fdft(SD<float> d, const float2* __restrict__ dft,
+                                              FdftPlan pl) {
+  constexpr int Q = I / 4;
+  const int J = d.J, K = d.K, M = d.M, NR9 = fdft_rows(K);
+  const int LC = pl.lc, RP = pl.rp, PS = pl.ps, NPP = pl.npp, TS = pl.ts;
+  const int nt = blockDim.x, nwarp = pl.warps;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const FdftLayout L(I, M, LC);
+  const int nch = (K + LC - 1) / LC, nunits = d.E * J * nch;
   extern __shared__ float4 sm4[];
   float* sm = reinterpret_cast<float*>(sm4);
-  float4* tab = reinterpret_cast<float4*>(sm + L.tab);     // [NP][Q+1]
-  float* raw = sm + L.raw;                                 // [rows][I]
-  float4* fw = reinterpret_cast<float4*>(sm + L.fw);       // [rows][Q+1]
-  float2* fout = reinterpret_cast<float2*>(sm + L.fout);   // [LC*7][M]
-  for (int x = tid; x < NP * (Q + 1); x += NT) {
-    const int p = x / (Q + 1), i = x - p * (Q + 1);
-    const float2 te = dft[(2 * p) * (Q + 1) + i];
-    const float2 to = (2 * p + 1 < M) ? dft[(2 * p + 1) * (Q + 1) + i] : make_float2(0.f, 0.f);
-    tab[x] = make_float4(te.x, te.y, to.x, to.y);
+  float* tab = sm + pl.tab;                 // [4][Q][NPP] (plane stride TS)
+  float* pln = sm + pl.pl;                  // [4][Q][RP] (plane stride PS); later the sums
+  float4* b0s = reinterpret_cast<float4*>(sm + pl.b0);   // [rows] (x0, x_{I/2}, u_Q, v_Q)
+
+  for (int x = tid; x < Q * NPP; x += nt) {
+    const int i = x / NPP, p = x - i * NPP;
+    const int me = 2 * p, mo = 2 * p + 1;
+    const float2 te = me < M ? dft[me * (Q + 1) + i] : make_float2(0.f, 0.f);
+    const float2 to = mo < M ? dft[mo * (Q + 1) + i] : make_float2(0.f, 0.f);
+    tab[0 * TS + x] = te.x;
+    tab[1 * TS + x] = te.y;
+    tab[2 * TS + x] = to.x;
+    tab[3 * TS + x] = to.y;
   }
-  const float gw = d.jfac[JF_GW * J + j], gwdc = d.jfac[JF_GWDELC * J + j];
-  const float wg = gw / float(I), wd = gwdc / float(I);
-  const float* g9 = d.grid9 + ((size_t)e * J + j) * fdft_rows(K) * I;
-  float2* afe = reinterpret_cast<float2*>(d.af) + (size_t)e * M * J * K * AF_N;
-  // rows of the chunk at k0: level rows 0 .. 9 lc - 1, then (first chunk)
-  // the two surface rows
-  auto stage = [&](int k0) {
-    const int lc = min(LC, K - k0);
-    const float* src = g9 + (size_t)(2 + 9 * k0) * I;
-    const int n4 = 9 * lc * I / 4;
-    for (int x = tid; x < n4; x += NT) cp_async16(raw + 4 * x, src + 4 * x);
-    if (k0 == 0)
-      for (int x = tid; x < 2 * I / 4; x += NT) cp_async16(raw + 9 * lc * I + 4 * x, g9 + 4 * x);
-    cp_async_commit();
-  };
-  stage(0);
-  for (int k0 = 0; k0 < K; k0 += LC) {
-    const int lc = min(LC, K - k0);
-    const bool surf = (k0 == 0);
+
+  // unit u: level chunk u % nch of column u / nch (member-major, then latitude)
+  for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+    const int cu = u % nch, col = u / nch;
+    const int e = col / J, j = col - e * J;
+    const int k0 = cu * LC, lc = min(LC, K - k0);
+    const bool surf = (cu == 0);
     const int nrow = 9 * lc + (surf ? 2 : 0);
-    cp_async_wait<0>();
-    __syncthreads();
-    for (int x = tid; x < nrow * (Q + 1); x += NT) {
-      const int r = x / (Q + 1), i = x - r * (Q + 1);
-      const float* row = raw + r * I;
-      float4 v;
-      if (i == 0) {
-        const float xq = row[Q], x3q = row[3 * Q];
-        v = make_float4(row[0], row[I / 2], xq + x3q, xq - x3q);
-      } else if (i == Q) {
-        v = make_float4(0.f, 0.f, 0.f, 0.f);
-      } else {
-        const float xa = row[i], xb = row[I - i], xc = row[I / 2 - i], xd = row[I / 2 + i];
-        const float u = xa + xb, w = xa - xb, uh = xc + xd, vh = xc - xd;
-        v = make_float4(u + uh, u - uh, w - vh, w + vh);
-      }
-      fw[x] = v;
-    }
-    __syncthreads();
-    if (k0 + LC < K) stage(k0 + LC);             // next chunk streams in meanwhile
-    const int nq = fdft_quads(lc) + (surf ? 1 : 0);
-    for (int it = tid; it < nq * NP; it += NT) {
-      const int p = it % NP, q = it / NP;
-      // rows of quad q (-1: none)
-      int rw[4];
+    // unit rows: the level rows, then (level 0) the two surface rows
+    const float* g9 = d.grid9 + (size_t)col * NR9 * I;
+    const float* lev = g9 + (size_t)(2 + 9 * k0) * I;
+    __syncthreads();                         // the previous unit's sums are read
+    // fold: a lane takes one point of four consecutive plane rows (a warp:
+    // 32 points, or two row quads at I = 64) and stores each plane's four
+    // rows as one float4; the lanes of point 0 keep (x0, x_{I/2}, u_Q, v_Q).
+    // Plane rows: level l's gt xu g yu fu fv ke xv at 8 l .. 8 l + 7, then the
+    // yv rows of the levels, then (level 0) the two surface rows.
+    {
+      constexpr int PPW = Q < 32 ? Q : 32, SUB = 32 / PPW, NIW = Q / PPW;
+      const int nrq = (nrow + 3) >> 2;
+      const int nit = ((nrq + SUB - 1) / SUB) * NIW;
+      auto rowp = [&](int pr) -> const float* {
+        if (pr < 8 * lc) return lev + (size_t)(9 * (pr >> 3) + (pr & 7)) * I;
+        if (pr < 9 * lc) return lev + (size_t)(9 * (pr - 8 * lc) + 8) * I;
+        return g9 + (size_t)(pr - 9 * lc) * I;
+      };
+      for (int it = warp; it < nit; it += nwarp) {
+        const int rq = (it / NIW) * SUB + lane / PPW;
+        const int i = (it % NIW) * PPW + (lane & (PPW - 1));
+        if (rq < nrq) {
+          float xv[4][4];
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        if (q < 2 * lc) {
-          rw[t] = 9 * (q >> 1) + ((q & 1) ? 4 : 0) + t;
-        } else if (q < fdft_quads(lc)) {
-          const int l = 4 * (q - 2 * lc) + t;
-          rw[t] = l < lc ? 9 * l + 8 : -1;
-        } else {
-          rw[t] = t < 2 ? 9 * lc + t : -1;
-        }
-      }
-      const float4* w[4];
-#pragma unroll
-      for (int t = 0; t < 4; ++t) w[t] = fw + (rw[t] >= 0 ? rw[t] : 0) * (Q + 1);
-      float acc[4][4];
-#pragma unroll
-      for (int t = 0; t < 4; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
-      const float4* tb = tab + p * (Q + 1);
-#pragma unroll 4
-      for (int i = 1; i < Q; ++i) {
-        const float4 c = tb[i];
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          const float4 a = w[t][i];
-          acc[t][0] = fmaf(a.x, c.x, acc[t][0]);   // even m: cos
-          acc[t][1] = fmaf(a.z, c.y, acc[t][1]);   // even m: sin
-          acc[t][2] = fmaf(a.y, c.z, acc[t][2]);   // odd m: cos
-          acc[t][3] = fmaf(a.w, c.w, acc[t][3]);   // odd m: sin
-        }
-      }
-      const int me = 2 * p, mo = 2 * p + 1;
-      const float ce = (p & 1) ? -1.f : 1.f;            // (-1)^{me/2}
-      const float so = (((mo - 1) / 2) & 1) ? -1.f : 1.f;  // (-1)^{(mo-1)/2}
-      float2 Xe[4], Xo[4];
-#pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const float4 b0 = w[t][0];        // (x0, x_{I/2}, u_Q, v_Q)
-        Xe[t] = make_float2(acc[t][0] + b0.x + b0.y + ce * b0.z, -acc[t][1]);
-        Xo[t] = make_float2(acc[t][2] + b0.x - b0.y, -(acc[t][3] + so * b0.w));
-      }
-      // I X_m of the quad's rows -> weighted analysis inputs
-      for (int par = 0; par < 2; ++par) {
-        const int m = par ? mo : me;
-        if (m >= M) break;
-        const float2* X = par ? Xo : Xe;
-        const float rm = float(m);
-        if (q < 2 * lc) {
-          float2* o = fout + ((q >> 1) * AF_N) * M;
-          if ((q & 1) == 0) {
-            // a3 = wg X(gt) - wd i m X(xu); a5 = wg X(g) - wd i m X(yu)
-            o[AF_T * M + m] = make_float2(wg * X[0].x + wd * rm * X[1].y,
-                                          wg * X[0].y - wd * rm * X[1].x);
-            o[AF_Q * M + m] = make_float2(wg * X[2].x + wd * rm * X[3].y,
-                                          wg * X[2].y - wd * rm * X[3].x);
-          } else {
-            o[AF_FU * M + m] = make_float2(wd * X[0].x, wd * X[0].y);
-            o[AF_FV * M + m] = make_float2(wd * X[1].x, wd * X[1].y);
-            o[AF_KE * M + m] = make_float2(wg * X[2].x, wg * X[2].y);
-            o[AF_XV * M + m] = make_float2(wd * X[3].x, wd * X[3].y);
-          }
-        } else if (q < fdft_quads(lc)) {
           for (int t = 0; t < 4; ++t) {
-            const int l = 4 * (q - 2 * lc) + t;
-            if (l < lc) fout[(l * AF_N + AF_YV) * M + m] = make_float2(wd * X[t].x, wd * X[t].y);
+            const int r = 4 * rq + t;
+            if (r < nrow) {
+              const float* row = rowp(r);
+              xv[t][0] = __ldg(row + i);
+              xv[t][1] = __ldg(row + ((I - i) & (I - 1)));
+              xv[t][2] = __ldg(row + (I / 2 - i));
+              xv[t][3] = __ldg(row + (I / 2 + i));
+            } else {
+              xv[t][0] = xv[t][1] = xv[t][2] = xv[t][3] = 0.f;
+            }
           }
-        } else {
-          float2* o = reinterpret_cast<float2*>(d.afs) + (((size_t)e * M + m) * J + j) * 2;
-          o[0] = make_float2(X[0].x * wg, X[0].y * wg);
-          o[1] = make_float2(X[1].x * wg, X[1].y * wg);
+          float pv[4][4];
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            const float xa = xv[t][0], xb = xv[t][1], xc = xv[t][2], xd = xv[t][3];
+            const float uu = xa + xb, w = xa - xb, uh = xc + xd, vh = xc - xd;
+            pv[0][t] = uu + uh;
+            pv[1][t] = w - vh;
+            pv[2][t] = uu - uh;
+            pv[3][t] = w + vh;
+            const int r = 4 * rq + t;
+            if (i == 0 && r < nrow) {
+              const float* row = rowp(r);
+              const float xq = __ldg(row + Q), x3q = __ldg(row + 3 * Q);
+              b0s[r] = make_float4(xa, xc, xq + x3q, xq - x3q);
+            }
+          }
+          if (i != 0) {
+            float* o = pln + i * RP + 4 * rq;
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+              *reinterpret_cast<float4*>(o + c * PS) = make_float4(pv[c][0], pv[c][1], pv[c][2], pv[c][3]);
+          }
         }
       }
     }
     __syncthreads();
-    const int row = lc * AF_N;
-    for (int m = warp; m < M; m += NW) {
-      float2* dst = afe + ((size_t)m * J + j) * K * AF_N + (size_t)k0 * AF_N;
-      for (int c = lane; c < row; c += 32) dst[c] = fout[c * M + m];
+    if (tid == 0 && u + (int)gridDim.x < nunits) {
+      // the next unit's rows (contiguous level rows, surface rows) into L2
+      const int un = u + gridDim.x, cn = un % nch, coln = un / nch;
+      const int kn = cn * LC, lcn = min(LC, K - kn);
+      const float* gn = d.grid9 + (size_t)coln * NR9 * I;
+      prefetch_l2_bulk(gn + (size_t)(2 + 9 * kn) * I, 9u * lcn * I * sizeof(float));
+      if (cn == 0) prefetch_l2_bulk(gn, 2u * I * sizeof(float));
+    }
+
+    // plane sums: lane = plane c (quarter warp) x (row group, pair group)
+    const int c = lane >> 3, k = warp * 8 + (lane & 7);
+    const int npg = pl.npg;
+    const bool active = k < pl.nrg * npg;
+    const int rg = active ? k / npg : 0, pg = active ? k - rg * npg : 0;
+    // the sums start from the point-0 and point-I/4 terms of their plane:
+    // even m: x0 + x_{I/2} +- u_Q (re), 0 (im); odd m: x0 - x_{I/2} (re),
+    // +- v_Q (im); the sign is (-1)^p, p = 8 pg + q
+    float acc[8][8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const float4 b = b0s[8 * rg + r];
+      const float e0 = b.x + b.y;
+      float v0, v1;                            // q even, q odd
+      if (c == 0) { v0 = e0 + b.z; v1 = e0 - b.z; }
+      else if (c == 1) { v0 = 0.f; v1 = 0.f; }
+      else if (c == 2) { v0 = b.x - b.y; v1 = v0; }
+      else { v0 = b.w; v1 = -b.w; }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc[r][q] = (q & 1) ? v1 : v0;
+    }
+    if (active) {
+      const float* pa = pln + c * PS + 8 * rg;
+      const float* pt = tab + c * TS + 8 * pg;
+#pragma unroll 2
+      for (int i = 1; i < Q; ++i) {
+        const float4 a0 = *reinterpret_cast<const float4*>(pa + i * RP);
+        const float4 a1 = *reinterpret_cast<const float4*>(pa + i * RP + 4);
+        const float4 t0 = *reinterpret_cast<const float4*>(pt + i * NPP);
+        const float4 t1 = *reinterpret_cast<const float4*>(pt + i * NPP + 4);
+        const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const float tv[8] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w};
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+#pragma unroll
+          for (int q = 0; q < 8; ++q) acc[r][q] = fmaf(av[r], tv[q], acc[r][q]);
+      }
+    }
+    __syncthreads();                         // planes read: the staged outputs overwrite them
+
+    // Epilogue.  Quarters 0 and 1 (2 and 3) hold the real and imaginary sums
+    // of even (odd) m for the same tile; partners exchange half their pairs
+    // so that each holds X = (S_re, -S_im) of 8 rows by 4 pairs: the even
+    // quarter pairs 0-3 of its group, the odd quarter pairs 4-7.  A level's
+    // group gives its six fields (a3 = wg X(gt) - wd i m X(xu), a5 from g,
+    // yu; fu fv ke xv); the trailing groups give yv and the surface rows.
+    const float gw = d.jfac[JF_GW * J + j], gwdc = d.jfac[JF_GWDELC * J + j];
+    const float wg = gw / float(I), wd = gwdc / float(I);
+    float2* fo = reinterpret_cast<float2*>(pln);     // [M][7 lc]: item m lc + l at 7 (m lc + l)
+    const bool ev = (c & 1) == 0;
+    const int par = c >> 1;                          // 0: even m, 1: odd m
+    const int NP = (M + 1) >> 1;
+#pragma unroll
+    for (int rp = 0; rp < 4; ++rp) {
+      float re[2][4], im[2][4];
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float send = ev ? acc[2 * rp + h][4 + q] : acc[2 * rp + h][q];
+          const float recv = __shfl_xor_sync(0xffffffffu, send, 8);
+          re[h][q] = ev ? acc[2 * rp + h][q] : recv;
+          im[h][q] = ev ? recv : acc[2 * rp + h][4 + q];
+        }
+      if (!active) continue;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int p = 8 * pg + (ev ? 0 : 4) + q, m = 2 * p + par;
+        if (p >= NP || m >= M) continue;
+        // X_h = (re[h], -im[h])
+        if (rg < lc) {
+          float2* o = fo + AF_N * (m * lc + rg);
+          const float wdm = wd * float(m);
+          if (rp < 2) {
+            // rows (gt, xu) or (g, yu): wg X0 - wd i m X1
+            o[rp == 0 ? AF_T : AF_Q] = make_float2(wg * re[0][q] + wdm * -im[1][q],
+                                                   wg * -im[0][q] - wdm * re[1][q]);
+          } else if (rp == 2) {
+            o[AF_FU] = make_float2(wd * re[0][q], wd * -im[0][q]);
+            o[AF_FV] = make_float2(wd * re[1][q], wd * -im[1][q]);
+          } else {
+            o[AF_KE] = make_float2(wg * re[0][q], wg * -im[0][q]);
+            o[AF_XV] = make_float2(wd * re[1][q], wd * -im[1][q]);
+          }
+        } else {
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int pr = 8 * rg + 2 * rp + h;
+            if (pr < 9 * lc) {
+              fo[AF_N * (m * lc + (pr - 8 * lc)) + AF_YV] = make_float2(wd * re[h][q], wd * -im[h][q]);
+            } else if (surf && pr < 9 * lc + 2) {
+              float2* os = reinterpret_cast<float2*>(d.afs);
+              os[(((size_t)e * M + m) * J + j) * 2 + (pr - 9 * lc)] =
+                  make_float2(wg * re[h][q], wg * -im[h][q]);
+            }
+          }
+        }
+      }
+    }
+    const int nitem = M * lc;
+    __syncthreads();
+    {
+      // staged rows -> af, consecutive threads on consecutive addresses
+      const int RS = AF_N * lc;
+      const unsigned mg = (unsigned)((0x100000000ull + RS - 1) / RS);   // y / RS, y < 2^16
+      float2* afu = reinterpret_cast<float2*>(d.af) + (((size_t)e * M * J + j) * K + k0) * AF_N;
+      const size_t mstride = (size_t)J * K * AF_N;
+      for (int y = tid; y < AF_N * nitem; y += nt) {
+        const int m = __umulhi((unsigned)y, mg);
+        afu[m * mstride + (y - m * RS)] = fo[y];
+      }
     }
   }
 }

@@ -976,6 +976,33 @@ template <typename R> size_t impl_smem(int K) {
          sizeof(C2<R>) * 2 * (size_t)(IM_THREADS / K) * K;
 }
 
+// Grid of a persistent kernel: the CTAs that are resident at once on the
+// current device (from the occupancy calculator, cached per kernel, block
+// size, shared memory and device), at most `units`.
+inline int persistent_grid(const void* fn, int nt, size_t smem, int units) {
+  struct Entry { const void* fn; int nt, dev; size_t smem; int ctas; };
+  static std::mutex mu;
+  static Entry cache[32];
+  static int ncache = 0;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int ctas = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    for (int i = 0; i < ncache; ++i)
+      if (cache[i].fn == fn && cache[i].nt == nt && cache[i].dev == dev && cache[i].smem == smem)
+        ctas = cache[i].ctas;
+    if (!ctas) {
+      int sms = 0, per = 0;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, nt, smem);
+      ctas = (sms > 0 ? sms : 1) * (per > 0 ? per : 1);
+      if (ncache < 32) cache[ncache++] = Entry{fn, nt, dev, smem, ctas};
+    }
+  }
+  return ctas < units ? ctas : units;
+}
+
 template <typename R, int I> int launch_step(const SD<R>& d, const lbm_step_ctl& c,
                                              cudaStream_t st, int only = -1) {
   constexpr int KB = grid_kb<R, I>(), NT = grid_nt<R, I>();
@@ -991,9 +1018,11 @@ template <typename R, int I> int launch_step(const SD<R>& d, const lbm_step_ctl&
     if (only < 0 || only == 0 || only == 5)
       k_alg<I><<<dim3(d.J, d.E), I, 0, st>>>(d, c.ps_mode);
     if (only < 0 || only == 0 || only == 6) {
-      const int lc = fdft_chunk(I, d.M, d.K);
-      k_fdft<I><<<dim3(d.J, d.E), SPLIT_NT, sizeof(float) * (size_t)FdftLayout(I, d.M, lc).total,
-                  st>>>(d, d.dft, lc);
+      const FdftPlan pl = fdft_plan(I, d.M, d.K);
+      const size_t smem = sizeof(float) * (size_t)pl.total;
+      const int nunits = d.E * d.J * ((d.K + pl.lc - 1) / pl.lc);
+      k_fdft<I><<<persistent_grid((const void*)k_fdft<I>, pl.nt, smem, nunits), pl.nt, smem,
+                  st>>>(d, d.dft, pl);
     }
   } else {
     if (only < 0 || only == 0)
@@ -1020,8 +1049,12 @@ template <typename R, int I> void set_attrs(const SD<R>& d) {
   if constexpr (sizeof(R) == 4) {
     cudaFuncSetAttribute(k_idft<I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)idft_smem(I, d.M));
-    cudaFuncSetAttribute(k_fdft<I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(sizeof(float) * FdftLayout(I, d.M, fdft_chunk(I, d.M, d.K)).total));
+    const FdftPlan pl = fdft_plan(I, d.M, d.K);
+    const size_t smem = sizeof(float) * (size_t)pl.total;
+    if (smem <= 227 * 1024) {
+      cudaFuncSetAttribute(k_fdft<I>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      persistent_grid((const void*)k_fdft<I>, pl.nt, smem, 1);
+    }
   } else {
     cudaFuncSetAttribute(k_grid<R, I, KB, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)GridSmem<R, I, KB, NT>::bytes(d.M));
@@ -1046,9 +1079,12 @@ template <typename R> int validate(const SD<R>& d) {
   for (int f = 0; f < 4; ++f)
     if (d.vd_on[f] && !d.vdiff) return LBM_ERR_ARG;
   if (sizeof(R) == 4 && (!d.dft || !d.grid6 || !d.grid9)) return LBM_ERR_ARG;
+  // 16-byte copies and bulk prefetches read sf, af and grid9
+  auto a16 = [](const void* p) { return ((uintptr_t)p & 15) == 0; };
+  if (!a16(d.sf) || !a16(d.af) || (sizeof(R) == 4 && !a16(d.grid9))) return LBM_ERR_ARG;
   if (sizeof(R) == 4 &&
       (idft_smem(d.I, d.M) > 227 * 1024 ||
-       sizeof(float) * (size_t)FdftLayout(d.I, d.M, fdft_chunk(d.I, d.M, d.K)).total > 227 * 1024))
+       sizeof(float) * (size_t)fdft_plan(d.I, d.M, d.K).total > 227 * 1024))
     return LBM_ERR_ARG;
   return LBM_OK;
 }

@@ -3,12 +3,15 @@
 ``LBM.run`` has two loops with the reference's step semantics
 (model.py:213-290):
 
-* the fused loop (default when no history writer is given): the whole
-  ensemble advances in the lbm_gb300 fused stepper with the state in packed
-  spectral space; steady-state steps replay as CUDA graphs; the blow-up
-  check reads a device flag once per model day instead of synchronising
-  every step, and reports the day in which a non-finite value appeared;
-* the general loop (history writer, or ``Config.fused=False``): one call of
+* the fused loop (default): the whole ensemble advances in the lbm_gb300
+  fused stepper with the state in packed spectral space; steady-state steps
+  replay as CUDA graphs; the blow-up check reads a device flag once per
+  model day instead of synchronising every step, and reports the day in
+  which a non-finite value appeared; with a history writer the stepper
+  accumulates the trapezoid of the spectral state and grid ps' each step
+  and the daily fields are formed once per day from the mean;
+* the general loop (a history writer with a non-zero initial state, or
+  ``Config.fused=False``): one call of
   ``Dynamics.tendencies``, ``State.to_spectral``, ``Integrator.step``,
   ``State.load_spectral`` and the Robert-Asselin filter per step, each
   backed by the library's reference-layout kernels, exactly as the
