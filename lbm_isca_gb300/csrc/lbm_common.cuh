@@ -10,6 +10,15 @@
 
 namespace lbm {
 
+// x / d by a multiply-high with m = ceil(2^32 / d): exact for 0 <= x < 2^32 / d
+// (the error x (m d - 2^32) / 2^32 stays below 1 / d there).
+struct FastDiv {
+  unsigned m;
+  int d;
+  LBM_D explicit FastDiv(int dv) : m((unsigned)((0x100000000ull + dv - 1) / dv)), d(dv) {}
+  LBM_D int div(int x) const { return d == 1 ? x : (int)__umulhi((unsigned)x, m); }
+};
+
 // Complex numbers as (re, im) pairs of the working precision.
 template <typename R> struct C2 { R x, y; };
 

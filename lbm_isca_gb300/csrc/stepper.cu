@@ -362,6 +362,10 @@ template <typename R> struct PairRows {
   LBM_D int n_of(int r) const { return r < L1 ? m1 + r : m2 + (r - L1); }
 };
 
+// Row groups of the analysis block: NC rows of an m-pair's N + 2 (at most
+// two partial groups).
+template <int NC> LBM_HD int anal_groups(int N) { return (N + 2 + NC - 1) / NC + 1; }
+
 template <typename R, int NC, int KC>
 __global__ void k_anal(SD<R> d) {
   const int p = blockIdx.x, e = blockIdx.y, kc = blockIdx.z;
@@ -369,23 +373,35 @@ __global__ void k_anal(SD<R> d) {
   const int k0 = kc * KC, kn = min(KC, K - k0);
   const PairRows<R> pr(p, N);
   const int G1 = (pr.L1 + NC - 1) / NC, G2 = (pr.L2 + NC - 1) / NC;
+  const int G = anal_groups<NC>(N);                    // row groups of the block
+  const int TS = NC * G + 1;                           // odd latitude stride of the tables
   extern __shared__ unsigned char smraw[];
-  R* tp = reinterpret_cast<R*>(smraw);                 // [NR][JH]
-  R* th = tp + pr.NR * JH;                             // [NR][JH]
+  // P and H of the pair's rows as [JH][NC][G]: row rbase(g) + i at slot i G + g,
+  // so the row groups of a warp read adjacent words (no bank conflict)
+  R* tp = reinterpret_cast<R*>(smraw);
+  R* th = tp + (size_t)JH * TS;
   // rows of AN_JC latitude pairs, two buffers, each
-  // [2 m][AN_JC][2 hemispheres][KC levels][7 fields] (an odd stride of 7
-  // complex values between lanes: no bank conflicts)
-  // (16-byte aligned)
+  // [2 m][AN_JC][2 hemispheres][KC levels][7 fields] (16-byte aligned)
   C2<R>* raw = reinterpret_cast<C2<R>*>(
-      (reinterpret_cast<uintptr_t>(th + pr.NR * JH) + 15) & ~uintptr_t(15));
+      (reinterpret_cast<uintptr_t>(th + (size_t)JH * TS) + 15) & ~uintptr_t(15));
   const int tid = threadIdx.x, nt = blockDim.x;
-  // tables for the pair's rows
   const int off1 = spec_offset(pr.m1, N), off2 = spec_offset(pr.m2, N);
-  for (int idx = tid; idx < pr.NR * JH; idx += nt) {
-    const int r = idx / JH, jh = idx % JH;
-    const int row = r < pr.L1 ? off1 + r : off2 + (r - pr.L1);
-    tp[idx] = d.symp[(size_t)row * JH + jh];
-    th[idx] = d.symh[(size_t)row * JH + jh];
+  {
+    const FastDiv fjh(JH), fg(G);
+    for (int idx = tid; idx < NC * G * JH; idx += nt) {
+      const int sl = fjh.div(idx), jh = idx - sl * JH;     // latitude fastest
+      const int i = fg.div(sl), gg = sl - i * G;
+      int row = -1;
+      if (gg < G1) {
+        const int r = gg * NC + i;
+        if (r < pr.L1) row = off1 + r;
+      } else if (gg < G1 + G2) {
+        const int r = (gg - G1) * NC + i;
+        if (r < pr.L2) row = off2 + r;
+      }
+      tp[jh * TS + sl] = row >= 0 ? d.symp[(size_t)row * JH + jh] : R(0);
+      th[jh * TS + sl] = row >= 0 ? d.symh[(size_t)row * JH + jh] : R(0);
+    }
   }
   const int k = tid % KC, g = tid / KC;
   const bool active = (k < kn) && (g < G1 + G2);
@@ -407,14 +423,17 @@ __global__ void k_anal(SD<R> d) {
   constexpr int PER = 16 / (int)sizeof(C2<R>);
   const bool wide = ((K * AF_N) % PER == 0) && ((k0 * AF_N) % PER == 0) &&
                     (rowlen % PER == 0) && (rowst % PER == 0);
+  const int step = wide ? PER : 1;
+  const int nchunk = rowlen / step;
+  const FastDiv fch(nchunk);
   auto prefetch = [&](int jh0, int b) {
     const int jc = min(AN_JC, JH - jh0);
     C2<R>* rb = raw + b * rawbuf;
-    const int step = wide ? PER : 1;
-    const int nchunk = rowlen / step;
-    for (int x = tid; x < nm * jc * 2 * nchunk; x += nt) {
-      const int c = (x % nchunk) * step, w = x / nchunk;
-      const int hemi = w & 1, jj = (w >> 1) % jc, mm = (w >> 1) / jc;
+    // rows w = (mm AN_JC + jj) 2 + hemi; those with jj >= jc are skipped
+    for (int x = tid; x < nm * AN_JC * 2 * nchunk; x += nt) {
+      const int w = fch.div(x), c = (x - w * nchunk) * step;
+      const int hemi = w & 1, jj = (w >> 1) & (AN_JC - 1), mm = w / (2 * AN_JC);
+      if (jj >= jc) continue;
       const int m = mm ? pr.m2 : pr.m1;
       const int jn = jh0 + jj, j = hemi ? J - 1 - jn : jn;
       C2<R>* dst = rb + ((mm * AN_JC + jj) * 2 + hemi) * rowst + c;
@@ -450,7 +469,7 @@ __global__ void k_anal(SD<R> d) {
         for (int i = 0; i < NC; ++i) {
           const int r = rbase + i;
           if (r >= rend) break;
-          const R P = tp[r * JH + jh], H = th[r * JH + jh];
+          const R P = tp[jh * TS + i * G + g], H = th[jh * TS + i * G + g];
           const int ps = (i & 1);          // parity of (n - m): rows alternate
           const int hs = ps ^ 1;
           cfma(acc[i][0], P, x[AF_FU][ps]);
@@ -506,8 +525,10 @@ __global__ void k_anal(SD<R> d) {
     const int m = pr.m_of(r), n = pr.n_of(r), mm = r < pr.L1 ? 0 : 1;
     const int par = (n - m) & 1;
     C2<R> a0 = cmk<R>(0, 0), a1 = cmk<R>(0, 0);
+    const int rr = r < pr.L1 ? r : r - pr.L1;
+    const int sl = (rr % NC) * G + (r < pr.L1 ? 0 : G1) + rr / NC;   // table slot of row r
     for (int jh = 0; jh < JH; ++jh) {
-      const R P = tp[r * JH + jh];
+      const R P = tp[jh * TS + sl];
       const C2<R>* x = ss + ((mm * JH + jh) * 2) * 2;
       cfma(a0, P, x[0 * 2 + par]);
       cfma(a1, P, x[1 * 2 + par]);
@@ -939,25 +960,27 @@ template <typename R, int I> constexpr int grid_nt() {
   return I == 64 ? 128 : ((I == 256 && sizeof(R) == 8) ? 128 : 256);
 }
 
-template <typename R> size_t anal_smem(int NR, int JH, int KC) {
-  return sizeof(R) * 2 * (size_t)NR * JH + 16 +
-         sizeof(C2<R>) * (size_t)2 * (2 * AN_JC * 2 * AF_N * KC);
+template <typename R> size_t anal_smem(int N, int JH, int KC) {
+  constexpr int NC = Cfg<R>::NC;
+  const size_t TS = (size_t)NC * anal_groups<NC>(N) + 1;
+  return sizeof(R) * 2 * TS * JH + 16 + sizeof(C2<R>) * (size_t)2 * (2 * AN_JC * 2 * AF_N * KC);
 }
 // Level chunk of the analysis block (one thread per level and row group): the
 // preferred Cfg<R>::KCA, halved where that block would exceed 256 threads.
 template <typename R> int anal_kc(int N) {
   constexpr int NC = Cfg<R>::NC;
-  const int G = (N + 2 + NC - 1) / NC + 1;
+  const int G = anal_groups<NC>(N);
   return (Cfg<R>::KCA * G > 256) ? Cfg<R>::KCA / 2 : Cfg<R>::KCA;
 }
 template <typename R, int KC> void launch_anal(const SD<R>& d, cudaStream_t st, bool attrs) {
   constexpr int NC = Cfg<R>::NC;
   const int JH = d.J / 2, NRmax = d.N + 2, NP = (d.M + 1) / 2;
-  const int G = (d.N + 2 + NC - 1) / NC + 1;
+  const int G = anal_groups<NC>(d.N);
   const int nt = ((KC * G + 31) / 32) * 32;
   // the surface pass also needs 2 * JH * 2 staging elements
-  size_t sm = anal_smem<R>(NRmax, JH, KC);
-  const size_t sm2 = sizeof(R) * 2 * (size_t)NRmax * JH + 16 + sizeof(C2<R>) * (size_t)2 * JH * 2 * 2;
+  size_t sm = anal_smem<R>(d.N, JH, KC);
+  const size_t sm2 = sizeof(R) * 2 * ((size_t)NC * G + 1) * JH + 16 +
+                     sizeof(C2<R>) * (size_t)2 * JH * 2 * 2;
   if (sm2 > sm) sm = sm2;
   if (attrs)
     cudaFuncSetAttribute(k_anal<R, NC, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -1127,7 +1150,7 @@ template <typename R> int prepare_attrs(const lbm_stepper_desc* desc) {
     // the analysis block holds one thread per (level, row group) of an m-pair
     constexpr int NC = Cfg<R>::NC;
     const int KC = anal_kc<R>(d.N);
-    const int G = (d.N + 2 + NC - 1) / NC + 1;
+    const int G = anal_groups<NC>(d.N);
     const int nt = ((KC * G + 31) / 32) * 32;
     cudaFuncAttributes fa;
     const cudaError_t ea = (KC == Cfg<R>::KCA)
