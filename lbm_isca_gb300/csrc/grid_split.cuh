@@ -20,7 +20,7 @@
 
 namespace lbm {
 
-constexpr int SPLIT_NT = 256;
+constexpr int IDFT_NT = 128;    // threads of the longitude synthesis block
 constexpr int IDFT_RC = 64;      // rows per staged chunk
 constexpr int IDFT_RG = 8;       // rows per thread item
 
@@ -35,8 +35,8 @@ LBM_HD size_t idft_smem(int I, int M) {
 
 // ---------------------------------------------------------------------------
 template <int I>
-__global__ void __launch_bounds__(SPLIT_NT) k_idft(SD<float> d, const float2* __restrict__ dft) {
-  constexpr int Q = I / 4, NT = SPLIT_NT, RC = IDFT_RC, RG = IDFT_RG;
+__global__ void __launch_bounds__(IDFT_NT) k_idft(SD<float> d, const float2* __restrict__ dft) {
+  constexpr int Q = I / 4, NT = IDFT_NT, RC = IDFT_RC, RG = IDFT_RG;
   const int j = blockIdx.x, e = blockIdx.y;
   const int J = d.J, K = d.K, M = d.M;
   const int NR = idft_rows(K);
@@ -96,53 +96,69 @@ __global__ void __launch_bounds__(SPLIT_NT) k_idft(SD<float> d, const float2* __
     cp_async_wait<1>();
     __syncthreads();
     const float2* F = fin + buf * M * RC;
-    // points i = 1..Q, RG rows per item: x_i, x_{I-i}, x_{I/2-i}, x_{I/2+i}
-    constexpr int NGR = RC / RG;
-    for (int it = tid; it < Q * NGR; it += NT) {
-      const int i = it % Q + 1, g = it / Q;
+    // points i and i + Q/2 (1 <= i <= Q/2), RG rows per item: each point
+    // gives x_i, x_{I-i}, x_{I/2-i}, x_{I/2+i}; a row value read from shared
+    // memory serves both points
+    constexpr int NGR = RC / RG, QH = Q / 2;
+    for (int it = tid; it < QH * NGR; it += NT) {
+      const int i0 = it % QH + 1, g = it / QH;
       const int r0 = g * RG;
       if (r0 >= nr) continue;
-      float ce[RG], co[RG], se[RG], so[RG];
+      float ce[2][RG], co[2][RG], se[2][RG], so[2][RG];
 #pragma unroll
-      for (int r = 0; r < RG; ++r) ce[r] = co[r] = se[r] = so[r] = 0.f;
-      const float2* tb = tab + i;
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int r = 0; r < RG; ++r) ce[h][r] = co[h][r] = se[h][r] = so[h][r] = 0.f;
+      const float2* tb0 = tab + i0;
+      const float2* tb1 = tab + i0 + QH;
       int m = 1;
       for (; m + 1 < M; m += 2) {              // (odd, even) pairs of m >= 1
-        const float2 to = tb[m * (Q + 1)], te = tb[(m + 1) * (Q + 1)];
+        const float2 to0 = tb0[m * (Q + 1)], te0 = tb0[(m + 1) * (Q + 1)];
+        const float2 to1 = tb1[m * (Q + 1)], te1 = tb1[(m + 1) * (Q + 1)];
         const float4* xo = reinterpret_cast<const float4*>(F + m * RC + r0);
         const float4* xe = reinterpret_cast<const float4*>(F + (m + 1) * RC + r0);
 #pragma unroll
         for (int t = 0; t < RG / 2; ++t) {
           const float4 b = xo[t], a = xe[t];
-          co[2 * t] = fmaf(b.x, to.x, co[2 * t]);       so[2 * t] = fmaf(b.y, to.y, so[2 * t]);
-          co[2 * t + 1] = fmaf(b.z, to.x, co[2 * t + 1]); so[2 * t + 1] = fmaf(b.w, to.y, so[2 * t + 1]);
-          ce[2 * t] = fmaf(a.x, te.x, ce[2 * t]);       se[2 * t] = fmaf(a.y, te.y, se[2 * t]);
-          ce[2 * t + 1] = fmaf(a.z, te.x, ce[2 * t + 1]); se[2 * t + 1] = fmaf(a.w, te.y, se[2 * t + 1]);
+          co[0][2 * t] = fmaf(b.x, to0.x, co[0][2 * t]);       so[0][2 * t] = fmaf(b.y, to0.y, so[0][2 * t]);
+          co[0][2 * t + 1] = fmaf(b.z, to0.x, co[0][2 * t + 1]); so[0][2 * t + 1] = fmaf(b.w, to0.y, so[0][2 * t + 1]);
+          ce[0][2 * t] = fmaf(a.x, te0.x, ce[0][2 * t]);       se[0][2 * t] = fmaf(a.y, te0.y, se[0][2 * t]);
+          ce[0][2 * t + 1] = fmaf(a.z, te0.x, ce[0][2 * t + 1]); se[0][2 * t + 1] = fmaf(a.w, te0.y, se[0][2 * t + 1]);
+          co[1][2 * t] = fmaf(b.x, to1.x, co[1][2 * t]);       so[1][2 * t] = fmaf(b.y, to1.y, so[1][2 * t]);
+          co[1][2 * t + 1] = fmaf(b.z, to1.x, co[1][2 * t + 1]); so[1][2 * t + 1] = fmaf(b.w, to1.y, so[1][2 * t + 1]);
+          ce[1][2 * t] = fmaf(a.x, te1.x, ce[1][2 * t]);       se[1][2 * t] = fmaf(a.y, te1.y, se[1][2 * t]);
+          ce[1][2 * t + 1] = fmaf(a.z, te1.x, ce[1][2 * t + 1]); se[1][2 * t + 1] = fmaf(a.w, te1.y, se[1][2 * t + 1]);
         }
       }
       if (m < M) {                              // last (odd) m
-        const float2 to = tb[m * (Q + 1)];
+        const float2 to0 = tb0[m * (Q + 1)], to1 = tb1[m * (Q + 1)];
         const float4* xo = reinterpret_cast<const float4*>(F + m * RC + r0);
 #pragma unroll
         for (int t = 0; t < RG / 2; ++t) {
           const float4 b = xo[t];
-          co[2 * t] = fmaf(b.x, to.x, co[2 * t]);       so[2 * t] = fmaf(b.y, to.y, so[2 * t]);
-          co[2 * t + 1] = fmaf(b.z, to.x, co[2 * t + 1]); so[2 * t + 1] = fmaf(b.w, to.y, so[2 * t + 1]);
+          co[0][2 * t] = fmaf(b.x, to0.x, co[0][2 * t]);       so[0][2 * t] = fmaf(b.y, to0.y, so[0][2 * t]);
+          co[0][2 * t + 1] = fmaf(b.z, to0.x, co[0][2 * t + 1]); so[0][2 * t + 1] = fmaf(b.w, to0.y, so[0][2 * t + 1]);
+          co[1][2 * t] = fmaf(b.x, to1.x, co[1][2 * t]);       so[1][2 * t] = fmaf(b.y, to1.y, so[1][2 * t]);
+          co[1][2 * t + 1] = fmaf(b.z, to1.x, co[1][2 * t + 1]); so[1][2 * t + 1] = fmaf(b.w, to1.y, so[1][2 * t + 1]);
         }
       }
 #pragma unroll
-      for (int r = 0; r < RG; ++r) {
-        if (r0 + r >= nr) break;
-        const int v = v0 + r0 + r;
-        const float sc = rscale(v);
-        const float c0 = F[r0 + r].x + 2.f * ce[r], c1 = 2.f * co[r];
-        const float s0 = 2.f * se[r], s1 = 2.f * so[r];
-        const float p = c0 + c1, mn = c0 - c1, s = s0 + s1, dd = s0 - s1;
-        float* row = g6 + (size_t)v * I;
-        row[i] = (p - s) * sc;
-        row[I - i] = (p + s) * sc;
-        row[I / 2 - i] = (mn + dd) * sc;
-        row[I / 2 + i] = (mn - dd) * sc;
+      for (int h = 0; h < 2; ++h) {
+        const int i = i0 + h * QH;
+#pragma unroll
+        for (int r = 0; r < RG; ++r) {
+          if (r0 + r >= nr) break;
+          const int v = v0 + r0 + r;
+          const float sc = rscale(v);
+          const float c0 = F[r0 + r].x + 2.f * ce[h][r], c1 = 2.f * co[h][r];
+          const float s0 = 2.f * se[h][r], s1 = 2.f * so[h][r];
+          const float p = c0 + c1, mn = c0 - c1, s = s0 + s1, dd = s0 - s1;
+          float* row = g6 + (size_t)v * I;
+          row[i] = (p - s) * sc;
+          row[I - i] = (p + s) * sc;
+          row[I / 2 - i] = (mn + dd) * sc;
+          row[I / 2 + i] = (mn - dd) * sc;
+        }
       }
     }
     // i = 0 and i = I/2: one row per thread (consecutive rows, no bank conflicts)

@@ -1037,7 +1037,7 @@ template <typename R, int I> int launch_step(const SD<R>& d, const lbm_step_ctl&
     // grid-point part as three launches: longitude synthesis, column
     // algebra, longitude analysis (kernel ids 4, 5, 6; 0 = all three)
     if (only < 0 || only == 0 || only == 4)
-      k_idft<I><<<dim3(d.J, d.E), SPLIT_NT, idft_smem(I, d.M), st>>>(d, d.dft);
+      k_idft<I><<<dim3(d.J, d.E), IDFT_NT, idft_smem(I, d.M), st>>>(d, d.dft);
     if (only < 0 || only == 0 || only == 5)
       k_alg<I><<<dim3(d.J, d.E), I, 0, st>>>(d, c.ps_mode);
     if (only < 0 || only == 0 || only == 6) {
