@@ -292,6 +292,36 @@ int lbm_graph_destroy(lbm_graph* g);
 int lbm_history_accumulate(int prec, int64_t n, const void* cur, void* prev,
                            double* acc, double w, int mode, void* stream);
 
+/* GrADS history records of one output day (replaces the record loop of
+ * GradsWriter.add, output.py:46-71).  fields is a host array of 8 device
+ * pointers to FP64 grid fields: psi, chi, u, v, w, t, z as [npts][kmax]
+ * (latitude, longitude, level; level fastest) and ps as [npts].  For each
+ * level of the first seven, then for ps, one Fortran sequential record: a
+ * big-endian int32 byte count 4 npts, npts big-endian IEEE float32 values
+ * (rounded to nearest), the count again.  With apply_z, z gets zfac * ps
+ * added first (zfac = 100 / (rho0 g), output.py:64-65).  out holds
+ * (7 kmax + 1) (npts + 2) uint32 words. */
+int lbm_grads_records(int64_t npts, int kmax, const double* const* fields, int apply_z,
+                      double zfac, uint32_t* out, void* stream);
+
+/* ---- Basic-state preprocessing (basicstate.py), FP64, one thread per column --
+ * lbm_z2ps: surface pressure [hPa] from geopotential height z [ncol][nk]
+ *   (gpm, level 0 = the highest pressure) and surface height zs [ncol] (m;
+ *   NULL = 0) on the pressure levels plev [nk] (hPa): interpolation linear
+ *   in ln p between the first level above zs and the one below it
+ *   (basicstate.py:115-151).
+ * lbm_spline: natural cubic spline through (x [nk], z [ncol][nk]) with a
+ *   shared monotonic abscissa, evaluated at xi [ncol][nl] -> out [ncol][nl];
+ *   outside the data range the end value, or xmiss where omisb (beyond x_0)
+ *   or omist (beyond x_{nk-1}) is set (basicstate.py:176-238); nk <= 64.
+ * lbm_zonal_filter: x [nlat][nlon][nk] in place; mode 1 = zonal mean,
+ *   mode 2 = deviation from it (basicstate.py:165-173). */
+int lbm_z2ps(int64_t ncol, int nk, const double* z, const double* zs, const double* plev,
+             double* ps, void* stream);
+int lbm_spline(int64_t ncol, int nk, int nl, const double* x, const double* z, const double* xi,
+               double* out, int omisb, int omist, double xmiss, void* stream);
+int lbm_zonal_filter(int nlat, int nlon, int nk, double* x, int mode, void* stream);
+
 /* ---- Stepping without allocating -------------------------------------------
  * No counterpart in the reference, whose step functions allocate their work
  * arrays through the array backend on every call.

@@ -33,6 +33,11 @@ IDIM = IMAX + 1
 IJDIM = IDIM * JMAX
 NSPEC = (NMAX + 1) * (NMAX + 2) // 2
 
+# the 17 ERA5 pressure levels of the basic-state input files [hPa]
+# (constants.py:100-103)
+PLEV17 = np.array([1000., 925., 850., 700., 600., 500., 400., 300., 250.,
+                   200., 150., 100., 70., 50., 30., 20., 10.], dtype=np.float64)
+
 # L20 sigma half levels, index 0 = surface (constants.py:92-97)
 SIGM = np.array([
     1.000, 0.990, 0.970, 0.930, 0.870,

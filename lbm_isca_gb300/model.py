@@ -45,6 +45,15 @@ DDRAG_DEFAULT = [0.5, 0.5, 0.5, 5, 15, 20, 20, 20, 20, 20,
                  20, 20, 20, 20, 20, 20, 20, 20, 0.5, 0.5]
 
 
+def _emit(writer, day, fields):
+    """One history record: device tensors to a writer that takes them (the
+    GrADS writer packs its records on the device), host arrays otherwise."""
+    if getattr(writer, "accepts_device", False):
+        writer.add(day, dict(fields))
+    else:
+        writer.add(day, {k: asnumpy(v) for k, v in fields.items()})
+
+
 @dataclass
 class Config:
     """The reference's namelist knobs (model.py:34-86) plus GB300 switches."""
@@ -253,10 +262,10 @@ class LBM:
                 if advanced % out_every == 0:
                     day_done += 1
                     if cfg.time_average:
-                        writer.add(day_done, {k: asnumpy(v / nacc) for k, v in acc.items()})
+                        _emit(writer, day_done, {k: v / nacc for k, v in acc.items()})
                         acc, nacc = None, 0
                     else:
-                        writer.add(day_done, {k: asnumpy(v) for k, v in fields.items()})
+                        _emit(writer, day_done, fields)
             prev_top = cur_top
             if verbose and progress_every and advanced % progress_every == 0:
                 self._progress(t0)
@@ -420,7 +429,7 @@ class LBM:
                     if advanced % out_every == 0:
                         day_done += 1
                         fields = self._diagnostics_mean(*stp.hist_mean())
-                        writer.add(day_done, {k: asnumpy(v) for k, v in fields.items()})
+                        _emit(writer, day_done, fields)
                         stp.hist_reset()
                     if advanced % spd == 0 and not stp.check_finite():
                         raise FloatingPointError(
