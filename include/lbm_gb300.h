@@ -298,11 +298,11 @@ int lbm_history_accumulate(int prec, int64_t n, const void* cur, void* prev,
  * (latitude, longitude, level; level fastest) and ps as [npts].  For each
  * level of the first seven, then for ps, one Fortran sequential record: a
  * big-endian int32 byte count 4 npts, npts big-endian IEEE float32 values
- * (rounded to nearest), the count again.  With apply_z, z gets zfac * ps
- * added first (zfac = 100 / (rho0 g), output.py:64-65).  out holds
- * (7 kmax + 1) (npts + 2) uint32 words. */
+ * (rounded to nearest), the count again.  With apply_z, z gets
+ * (ps * zmul) / zdiv added first (zmul = 100, zdiv = rho0 g; output.py:64-65).
+ * out holds (7 kmax + 1) (npts + 2) uint32 words. */
 int lbm_grads_records(int64_t npts, int kmax, const double* const* fields, int apply_z,
-                      double zfac, uint32_t* out, void* stream);
+                      double zmul, double zdiv, uint32_t* out, void* stream);
 
 /* ---- Basic-state preprocessing (basicstate.py), FP64, one thread per column --
  * lbm_z2ps: surface pressure [hPa] from geopotential height z [ncol][nk]

@@ -33,7 +33,8 @@ BS_KEEP = ["z", "q", "t", "u", "v"]
 
 def _dev(a, device=None):
     dev = torch.device(device) if device is not None else torch.device("cuda")
-    t = a if isinstance(a, torch.Tensor) else torch.as_tensor(np.asarray(a, dtype=np.float64))
+    t = a if isinstance(a, torch.Tensor) else \
+        torch.from_numpy(np.array(a, dtype=np.float64, copy=True))
     if dev.type != "cuda":
         raise RuntimeError("basic-state kernels need a CUDA device (there is no CPU path)")
     return t.to(device=dev, dtype=torch.float64).contiguous()
@@ -55,9 +56,10 @@ def read_pressure_levels(path, kmo=1, navg=3, nlon=IMAX, nlat=JMAX, nlev=17,
     """Average ``navg`` months from month ``kmo`` (wrapping past the last one)
     of a pressure-level file: Fortran sequential records, big-endian real*4,
     one (nlon, nlat) field per record, ordered month -> variable -> level,
-    rows south first (``yflip`` turns them north first).  A point undefined
-    in any averaged month becomes ``XMISS``.  Returns (nlat, nlon, nlev)
-    arrays of z, q, t, u, v."""
+    rows south first (``yflip`` turns them north first).  A point equal to
+    ``UNDEF_IN`` in any averaged month becomes ``XMISS``; the comparison is
+    made on the values widened to double precision, as the reference makes
+    it.  Returns (nlat, nlon, nlev) arrays of z, q, t, u, v."""
     npts = nlon * nlat
     words = np.fromfile(path, dtype=">f4")
     if words.size % (npts + 2):
@@ -132,16 +134,17 @@ def spline(x, z, xi, omisb=False, omist=False, xmiss=XMISS):
 
 def _p2s_dev(gdi, ps, sig, plev=PLEV17, xmiss=XMISS):
     g = _dev(gdi)
-    nlat, nlon, nlevp = g.shape
+    lead, nlevp = tuple(g.shape[:-1]), g.shape[-1]
     lnp = torch.log(_dev(plev))
     lns = torch.log(_dev(ps).reshape(-1, 1) * _dev(sig).reshape(1, -1))
     out = _spline_dev(lnp, g.reshape(-1, nlevp), lns, xmiss=xmiss)
-    return out.reshape(nlat, nlon, -1)
+    return out.reshape(lead + (-1,))
 
 
 def p2s(gdi, ps, sig, plev=PLEV17, xmiss=XMISS):
     """Pressure -> sigma levels (basicstate.py:241-260): gdi (nlat, nlon,
-    nlevp) on ``plev``, ps (nlat, nlon) [hPa], sig (kmax,)."""
+    nlevp) on ``plev``, ps (nlat, nlon) [hPa], sig (kmax,).  Leading axes
+    beyond (nlat, nlon) -- several basic states at once -- are columns too."""
     return asnumpy(_p2s_dev(gdi, ps, sig, plev, xmiss))
 
 

@@ -4,7 +4,8 @@
 // Fortran sequential record per level of psi, chi, u, v, w, t, z and one of
 // ps: a big-endian int32 byte count, the field's npts values as big-endian
 // real*4, the byte count again.  z first gets the surface-pressure term
-// zfac * ps (output.py:64-65).  One thread per output word.
+// (ps * zmul) / zdiv, evaluated in that order (output.py:64-65).  One thread
+// per output word.
 
 #include "lbm_common.cuh"
 
@@ -15,7 +16,8 @@ struct GradsFields {
 };
 
 __global__ void k_grads_records(GradsFields g, long long npts, int kmax, int apply_z,
-                                double zfac, unsigned* __restrict__ out, long long nwords) {
+                                double zmul, double zdiv, unsigned* __restrict__ out,
+                                long long nwords) {
   const long long rl = npts + 2;                        // words per record
   const unsigned marker = __byte_perm((unsigned)(4 * npts), 0, 0x0123);
   for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nwords;
@@ -30,7 +32,7 @@ __global__ void k_grads_records(GradsFields g, long long npts, int kmax, int app
       if (rec < 7LL * kmax) {
         const int fld = (int)(rec / kmax), k = (int)(rec - (long long)fld * kmax);
         v = g.f[fld][i * kmax + k];
-        if (fld == 6 && apply_z) v += g.f[7][i] * zfac;
+        if (fld == 6 && apply_z) v += (g.f[7][i] * zmul) / zdiv;
       } else {
         v = g.f[7][i];
       }
@@ -45,8 +47,10 @@ __global__ void k_grads_records(GradsFields g, long long npts, int kmax, int app
 using namespace lbm;
 
 extern "C" int lbm_grads_records(int64_t npts, int kmax, const double* const* fields,
-                                 int apply_z, double zfac, uint32_t* out, void* stream) {
-  if (npts < 1 || kmax < 1 || !fields || !out || 4 * npts > 0x7fffffffLL) return LBM_ERR_ARG;
+                                 int apply_z, double zmul, double zdiv, uint32_t* out,
+                                 void* stream) {
+  if (npts < 1 || kmax < 1 || !fields || !out || 4 * npts > 0x7fffffffLL || zdiv == 0.0)
+    return LBM_ERR_ARG;
   GradsFields g;
   for (int i = 0; i < 8; ++i) {
     if (!fields[i]) return LBM_ERR_ARG;
@@ -56,8 +60,8 @@ extern "C" int lbm_grads_records(int64_t npts, int kmax, const double* const* fi
   const int nt = 256;
   long long nb = (nwords + nt - 1) / nt;
   if (nb > 4096) nb = 4096;
-  k_grads_records<<<(unsigned)nb, nt, 0, (cudaStream_t)stream>>>(g, npts, kmax, apply_z, zfac,
-                                                                   out, nwords);
+  k_grads_records<<<(unsigned)nb, nt, 0, (cudaStream_t)stream>>>(g, npts, kmax, apply_z, zmul,
+                                                                   zdiv, out, nwords);
   LBM_LAUNCH_CHECK();
   return LBM_OK;
 }

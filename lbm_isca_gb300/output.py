@@ -63,8 +63,8 @@ def grads_records(fields, apply_z=True, device="cuda"):
                              f"expected {(nlat, nlon, kmax)}")
     out = torch.empty((7 * kmax + 1) * (npts + 2), dtype=torch.int32, device=dev)
     ptrs = (C.c_void_p * 8)(*[t.data_ptr() for t in ts])
-    zfac = 1.0e2 / (RHO00 * GRAV_GT2GR)
-    check(lib().lbm_grads_records(npts, kmax, ptrs, 1 if apply_z else 0, zfac,
+    check(lib().lbm_grads_records(npts, kmax, ptrs, 1 if apply_z else 0, 1.0e2,
+                                  RHO00 * GRAV_GT2GR,
                                   C.c_void_p(out.data_ptr()),
                                   C.c_void_p(stream_handle(torch.cuda.current_stream(dev)))),
           "lbm_grads_records")
