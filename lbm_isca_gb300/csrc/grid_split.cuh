@@ -180,9 +180,13 @@ __global__ void __launch_bounds__(IDFT_NT) k_idft(SD<float> d, const float2* __r
 }
 
 // ---------------------------------------------------------------------------
-// One thread per column (blockDim = I).
+// One thread per column (blockDim = I).  The kernel waits on global loads;
+// the minimum resident blocks per SM keep 92 / 80 / 80 registers at I = 64 /
+// 128 / 256 -- at 128 that is six blocks instead of five, 10% faster at 512
+// members (seven and eight spill and are slower).
 template <int I>
-__global__ void __launch_bounds__(I) k_alg(SD<float> d, int ps_mode) {
+__global__ void __launch_bounds__(I, I == 64 ? 10 : (I == 128 ? 6 : 3))
+    k_alg(SD<float> d, int ps_mode) {
   const int j = blockIdx.x, e = blockIdx.y, c = threadIdx.x;
   const int J = d.J, K = d.K;
   __shared__ float vert[LBM_VERT_COUNT * 65];
