@@ -11,8 +11,9 @@
 //           hydrostatic prefix running in registers) -> grid9
 //           [E][J][2 + 9K][I] (gt_pi, pi(t-dt), then per level gt, xu, g, yu,
 //           fu, fv, ke, xv, yv), plus the grid ps Robert-Asselin update;
-//   k_fdft  per (latitude, member): the weighted longitude analysis of grid9
-//           -> af/afs.
+//   k_fdft  persistent CTAs over (member, latitude, level chunk) units: the
+//           weighted longitude analysis of grid9 -> af/afs as four
+//           register-tiled plane products (see the kernel).
 //
 // The longitude transforms are dense DFTs folded by quarter-wave symmetry:
 // the points i, I - i, I/2 - i, I/2 + i share |cos| and |sin| of every

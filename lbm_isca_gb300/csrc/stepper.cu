@@ -773,7 +773,7 @@ LBM_D void store_pair(C2<double>* o, C2<double> a, C2<double> b) {
 // =============================================================================
 constexpr int SY_THREADS = 320;
 
-template <typename R, int JG, int KC>
+template <typename R, int JG, int KC, int HV>
 __global__ void __launch_bounds__(SY_THREADS, 2) k_synth(SD<R> d) {
   const int p = blockIdx.x, e = blockIdx.y, kc = blockIdx.z;
   const int J = d.J, K = d.K, N = d.N, M = d.M, JH = J / 2, NS = d.NS;
@@ -812,62 +812,106 @@ __global__ void __launch_bounds__(SY_THREADS, 2) k_synth(SD<R> d) {
   const size_t jmK = (size_t)J * K;
   C2<R>* sfe = d.sf + (size_t)e * M * jmK * SF_N;
   const int nm = pr.L2 ? 2 : 1;
-  // one (level, latitude group) per item, both m of the pair in turn: every
-  // item walks N + 2 rows, so the pair's rows are balanced across threads
-  for (int it = tid; it < NJG * KC; it += nt) {
-    const int kk = it % KC;
-    const int jg = it / KC;
+  // Items: (term half, latitude group, level), level fastest.  With HV = 2
+  // the first NJG KC items take the wind terms (P chi, H psi, P psi, H chi ->
+  // U, V), the rest the scalar terms (P vor, P div, P T, P q): each value read
+  // from shared memory then feeds JG latitudes of four terms, and the halves
+  // are whole warps apart.  HV = 1: every item takes all eight terms.  Every
+  // item walks the N + 2 rows of both m of the pair, so the pair's rows are
+  // balanced across threads.
+  const int nhalf = NJG * KC;
+  for (int it = tid; it < HV * nhalf; it += nt) {
+    const int half = HV == 2 ? (it >= nhalf ? 1 : 0) : -1;
+    const int ri = it - (half > 0 ? nhalf : 0);
+    const int kk = ri % KC;
+    const int jg = ri / KC;
     if (kk >= kn) continue;
    for (int mm = 0; mm < nm; ++mm) {
     const int m = mm ? pr.m2 : pr.m1;
     const int rb = mm ? pr.L1 : 0, re = mm ? pr.NR : pr.L1;
-    // accumulators: [jg][term][plus/minus]; terms: Pchi Hpsi Ppsi Hchi Pvor Pdiv Pt Pq
-    C2<R> acc[JG][8][2];
-#pragma unroll
-    for (int a = 0; a < JG; ++a)
-#pragma unroll
-      for (int b = 0; b < 8; ++b) acc[a][b][0] = acc[a][b][1] = cmk<R>(0, 0);
+    const R rm = R(m);
     // rows alternate parity of (n - m), starting even; P of an even row is
     // symmetric about the equator (plus), H of an even row antisymmetric.
-    auto row = [&](int r, auto par_tag) {
-      constexpr int PP = decltype(par_tag)::value, HP = PP ^ 1;
-      const C2<R>* s = sv + r * 6 * KC + kk;
-      const C2<R> psi = s[0 * KC], chi = s[1 * KC], vo = s[2 * KC], dv = s[3 * KC];
-      const C2<R> tt = s[4 * KC], qq = s[5 * KC];
+    // acc[jg][term][plus/minus]
+    auto wind = [&]() {
+      C2<R> acc[JG][4][2];
+#pragma unroll
+      for (int a = 0; a < JG; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b][0] = acc[a][b][1] = cmk<R>(0, 0);
+      auto row = [&](int r, auto par_tag) {
+        constexpr int PP = decltype(par_tag)::value, HP = PP ^ 1;
+        const C2<R>* sr = sv + r * 6 * KC + kk;
+        const C2<R> psi = sr[0 * KC], chi = sr[1 * KC];
+#pragma unroll
+        for (int a = 0; a < JG; ++a) {
+          const int jh = min(jg * JG + a, JH - 1);
+          const R P = tp[r * JH + jh], H = th[r * JH + jh];
+          cfma(acc[a][0][PP], P, chi);
+          cfma(acc[a][1][HP], H, psi);
+          cfma(acc[a][2][PP], P, psi);
+          cfma(acc[a][3][HP], H, chi);
+        }
+      };
+      for (int r = rb; r < re; r += 2) {
+        row(r, std::integral_constant<int, 0>{});
+        if (r + 1 < re) row(r + 1, std::integral_constant<int, 1>{});
+      }
 #pragma unroll
       for (int a = 0; a < JG; ++a) {
-        const int jh = min(jg * JG + a, JH - 1);
-        const R P = tp[r * JH + jh], H = th[r * JH + jh];
-        cfma(acc[a][0][PP], P, chi);
-        cfma(acc[a][1][HP], H, psi);
-        cfma(acc[a][2][PP], P, psi);
-        cfma(acc[a][3][HP], H, chi);
-        cfma(acc[a][4][PP], P, vo);
-        cfma(acc[a][5][PP], P, dv);
-        cfma(acc[a][6][PP], P, tt);
-        cfma(acc[a][7][PP], P, qq);
+        const int jh = jg * JG + a;
+        if (jh >= JH) break;
+#pragma unroll
+        for (int hemi = 0; hemi < 2; ++hemi) {
+          const int j = hemi ? J - 1 - jh : jh;
+          const R sg = hemi ? R(-1) : R(1);
+          auto comb = [&](int b) { return acc[a][b][0] + acc[a][b][1] * sg; };
+          C2<R>* o = sfe + (((size_t)m * J + j) * K + k0 + kk) * SF_N;
+          store_pair(o + SF_U, im_mul(comb(0), rm) - comb(1), im_mul(comb(2), rm) + comb(3));
+        }
       }
     };
-    for (int r = rb; r < re; r += 2) {
-      row(r, std::integral_constant<int, 0>{});
-      if (r + 1 < re) row(r + 1, std::integral_constant<int, 1>{});
-    }
-    const R rm = R(m);
+    auto scalars = [&]() {
+      C2<R> acc[JG][4][2];
 #pragma unroll
-    for (int a = 0; a < JG; ++a) {
-      const int jh = jg * JG + a;
-      if (jh >= JH) break;
+      for (int a = 0; a < JG; ++a)
 #pragma unroll
-      for (int hemi = 0; hemi < 2; ++hemi) {
-        const int j = hemi ? J - 1 - jh : jh;
-        const R sg = hemi ? R(-1) : R(1);
-        auto comb = [&](int b) { return acc[a][b][0] + acc[a][b][1] * sg; };
-        C2<R>* o = sfe + (((size_t)m * J + j) * K + k0 + kk) * SF_N;
-        store_pair(o + SF_U, im_mul(comb(0), rm) - comb(1), im_mul(comb(2), rm) + comb(3));
-        store_pair(o + SF_VOR, comb(4), comb(5));
-        store_pair(o + SF_T, comb(6), comb(7));
+        for (int b = 0; b < 4; ++b) acc[a][b][0] = acc[a][b][1] = cmk<R>(0, 0);
+      auto row = [&](int r, auto par_tag) {
+        constexpr int PP = decltype(par_tag)::value;
+        const C2<R>* sr = sv + r * 6 * KC + kk;
+        const C2<R> vo = sr[2 * KC], dv = sr[3 * KC], tt = sr[4 * KC], qq = sr[5 * KC];
+#pragma unroll
+        for (int a = 0; a < JG; ++a) {
+          const int jh = min(jg * JG + a, JH - 1);
+          const R P = tp[r * JH + jh];
+          cfma(acc[a][0][PP], P, vo);
+          cfma(acc[a][1][PP], P, dv);
+          cfma(acc[a][2][PP], P, tt);
+          cfma(acc[a][3][PP], P, qq);
+        }
+      };
+      for (int r = rb; r < re; r += 2) {
+        row(r, std::integral_constant<int, 0>{});
+        if (r + 1 < re) row(r + 1, std::integral_constant<int, 1>{});
       }
-    }
+#pragma unroll
+      for (int a = 0; a < JG; ++a) {
+        const int jh = jg * JG + a;
+        if (jh >= JH) break;
+#pragma unroll
+        for (int hemi = 0; hemi < 2; ++hemi) {
+          const int j = hemi ? J - 1 - jh : jh;
+          const R sg = hemi ? R(-1) : R(1);
+          auto comb = [&](int b) { return acc[a][b][0] + acc[a][b][1] * sg; };
+          C2<R>* o = sfe + (((size_t)m * J + j) * K + k0 + kk) * SF_N;
+          store_pair(o + SF_VOR, comb(0), comb(1));
+          store_pair(o + SF_T, comb(2), comb(3));
+        }
+      }
+    };
+    if (half <= 0) wind();
+    if (half != 0) scalars();
    }
   }
   // surface fields (first level chunk only)
@@ -952,8 +996,12 @@ namespace lbm {
 
 // ---- launch configuration ------------------------------------------------------
 template <typename R> struct Cfg;
-template <> struct Cfg<float> { static constexpr int NC = 4, KCA = 20, JG = 2, KCS = 20; };
-template <> struct Cfg<double> { static constexpr int NC = 2, KCA = 10, JG = 1, KCS = 10; };
+template <> struct Cfg<float> {
+  static constexpr int NC = 4, KCA = 20, JG = 4, KCS = 20, SHV = 2;
+};
+template <> struct Cfg<double> {
+  static constexpr int NC = 2, KCA = 10, JG = 1, KCS = 10, SHV = 1;
+};
 
 template <typename R, int I> constexpr int grid_kb() { return (sizeof(R) == 8 && I == 256) ? 2 : 4; }
 template <typename R, int I> constexpr int grid_nt() {
@@ -993,6 +1041,16 @@ template <typename R> void run_anal(const SD<R>& d, cudaStream_t st, bool attrs)
 }
 template <typename R> size_t synth_smem(int NR, int JH) {
   return sizeof(R) * 2 * (size_t)NR * JH + sizeof(C2<R>) * (size_t)NR * Cfg<R>::KCS * 6;
+}
+// Legendre synthesis launch: HV NJG KC items, at most SY_THREADS threads.
+template <typename R> void launch_synth(const SD<R>& d, cudaStream_t st) {
+  constexpr int JG = Cfg<R>::JG, KC = Cfg<R>::KCS, HV = Cfg<R>::SHV;
+  const int JH = d.J / 2, NRmax = d.N + 2, NP = (d.M + 1) / 2;
+  const int NJG = (JH + JG - 1) / JG;
+  int nt = HV * NJG * KC;
+  nt = nt > SY_THREADS ? SY_THREADS : ((nt + 31) / 32) * 32;
+  k_synth<R, JG, KC, HV><<<dim3(NP, d.E, (d.K + KC - 1) / KC), nt, synth_smem<R>(NRmax, JH),
+                           st>>>(d);
 }
 template <typename R> size_t impl_smem(int K) {
   return sizeof(R) * ((size_t)(2 + 4) * K * K + 7 * (size_t)K + (K & 1)) +
@@ -1055,13 +1113,7 @@ template <typename R, int I> int launch_step(const SD<R>& d, const lbm_step_ctl&
   if (only < 0 || only == 2)
     k_implicit<R><<<dim3(NP, d.E), IM_THREADS, impl_smem<R>(d.K), st>>>(d, R(c.dt), c.set,
                                                                          c.ra_mode);
-  if (only < 0 || only == 3) {
-    constexpr int JG = Cfg<R>::JG, KC = Cfg<R>::KCS;
-    const int NJG = (JH + JG - 1) / JG;
-    int nt = NJG * KC;
-    nt = nt > SY_THREADS ? SY_THREADS : ((nt + 31) / 32) * 32;
-    k_synth<R, JG, KC><<<dim3(NP, d.E, (d.K + KC - 1) / KC), nt, synth_smem<R>(NRmax, JH), st>>>(d);
-  }
+  if (only < 0 || only == 3) launch_synth<R>(d, st);
   LBM_LAUNCH_CHECK();
   return LBM_OK;
 }
@@ -1085,7 +1137,7 @@ template <typename R, int I> void set_attrs(const SD<R>& d) {
   run_anal<R>(d, nullptr, true);
   cudaFuncSetAttribute(k_implicit<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)impl_smem<R>(d.K));
-  cudaFuncSetAttribute(k_synth<R, Cfg<R>::JG, Cfg<R>::KCS>,
+  cudaFuncSetAttribute(k_synth<R, Cfg<R>::JG, Cfg<R>::KCS, Cfg<R>::SHV>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)synth_smem<R>(NRmax, JH));
 }
@@ -1171,12 +1223,7 @@ template <typename R> int prime(const lbm_stepper_desc* desc, cudaStream_t st) {
   const SD<R> d = make_sd<R>(*desc);
   int rc = validate(d);
   if (rc) return rc;
-  constexpr int JG = Cfg<R>::JG, KC = Cfg<R>::KCS;
-  const int JH = d.J / 2, NRmax = d.N + 2, NP = (d.M + 1) / 2;
-  const int NJG = (JH + JG - 1) / JG;
-  int nt = NJG * KC;
-  nt = nt > SY_THREADS ? SY_THREADS : ((nt + 31) / 32) * 32;
-  k_synth<R, JG, KC><<<dim3(NP, d.E, (d.K + KC - 1) / KC), nt, synth_smem<R>(NRmax, JH), st>>>(d);
+  launch_synth<R>(d, st);
   LBM_LAUNCH_CHECK();
   return LBM_OK;
 }
