@@ -22,7 +22,7 @@
 namespace lbm {
 
 constexpr int IDFT_NT = 128;    // threads of the longitude synthesis block
-constexpr int IDFT_RC = 64;      // rows per staged chunk
+constexpr int IDFT_RC = 48;      // rows per staged chunk (two buffers fit five CTAs per SM)
 constexpr int IDFT_RG = 8;       // rows per thread item
 
 LBM_HD int idft_rows(int K) { return 6 + 6 * K; }
