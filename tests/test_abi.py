@@ -55,3 +55,24 @@ def test_noalloc_stepper_rejects_oversized_cases_without_a_device():
     d.nmem = 0
     assert L.lbm_stepper_run_noalloc(C.byref(d), ctl, 1, None) == _lib.LBM_ERR_ARG
     assert L.lbm_stepper_run_noalloc(None, ctl, 1, None) == _lib.LBM_ERR_ARG
+
+
+def test_io_and_setup_entry_points_reject_bad_arguments_without_a_device():
+    """History packing and basic-state column kernels validate before any
+    CUDA call."""
+    import ctypes as C
+    from lbm_isca_gb300 import _lib
+    L = _lib.lib()
+    VP = C.c_void_p
+    fake = VP(16)                      # never dereferenced: rejected first
+    ptrs = (VP * 8)(*([fake] * 8))
+    nulls = (VP * 8)()
+    assert L.lbm_grads_records(0, 20, ptrs, 1, 100.0, 12.0, fake, None) == _lib.LBM_ERR_ARG
+    assert L.lbm_grads_records(8192, 20, nulls, 1, 100.0, 12.0, fake, None) == _lib.LBM_ERR_ARG
+    assert L.lbm_grads_records(8192, 20, ptrs, 1, 100.0, 0.0, fake, None) == _lib.LBM_ERR_ARG
+    assert L.lbm_z2ps(0, 17, fake, None, fake, fake, None) == _lib.LBM_ERR_ARG
+    assert L.lbm_z2ps(10, 1, fake, None, fake, fake, None) == _lib.LBM_ERR_ARG
+    assert L.lbm_spline(10, 65, 5, fake, fake, fake, fake, 0, 0, -999.0, None) == _lib.LBM_ERR_ARG
+    assert L.lbm_spline(10, 17, 0, fake, fake, fake, fake, 0, 0, -999.0, None) == _lib.LBM_ERR_ARG
+    assert L.lbm_zonal_filter(32, 64, 20, fake, 3, None) == _lib.LBM_ERR_ARG
+    assert L.lbm_zonal_filter(32, 64, 20, None, 1, None) == _lib.LBM_ERR_ARG
