@@ -239,7 +239,7 @@ def algorithmic_bytes(E, p):
 
 def read_traffic(kernel, E):
     """dram bytes per launch from the committed ncu summary, scaled to E."""
-    path = os.path.join(ROOT, "profiles", "ncu_summary.md")
+    path = os.path.join(ROOT, "profiles", "fp32_stepper_t42l20.md")
     if not os.path.exists(path):
         return None
     key = f"traffic[{kernel}]"
