@@ -143,6 +143,10 @@ typedef struct lbm_tend_grid_args {
   int64_t frc_t_stride, frc_ps_stride, frc_q_stride;
   /* outputs: 3-D (R)[E][J][I][K], 2-D (R)[E][J][I]; omega may be NULL */
   void *fu, *fv, *ke, *gt, *xu, *xv, *g, *yu, *yv, *gt_pi, *omega, *sdot;
+  /* tangent-linear mode: when non-NULL, the kinetic-energy term
+   * 0.5 (u^2 + v^2) is replaced by its linearisation u0 u + v0 v about the
+   * trajectory (u0, v0) (R)[E][J][I][K]; both NULL = the model's own term */
+  const void *lin_u, *lin_v;
 } lbm_tend_grid_args;
 
 int lbm_tendency_grid(int prec, const lbm_tend_grid_args* a, void* stream);
@@ -166,6 +170,43 @@ typedef struct lbm_implicit_args {
 } lbm_implicit_args;
 
 int lbm_implicit_step(int prec, const lbm_implicit_args* a, void* stream);
+
+/* ============================================================================
+ * Adjoints of the two maps above (the transposes of their linearisations),
+ * for the hand-written adjoint of the time step.  Same layouts and sizes.
+ * ==========================================================================*/
+typedef struct lbm_tend_adj_args {
+  int nmem, nlat, nlon, kmax;
+  double kappa, epsvt, rair;
+  const void *dsig, *sigm, *alpha, *w3, *wP, *cpg, *ww, *tmtx, *tref;
+  const void *ub, *vb, *tb, *qb, *tvb, *absvor, *divb, *x5b, *sdotb, *pixb, *piyb;
+  /* trajectory (R)[E][J][I][K] of the kinetic-energy linearisation, or both
+   * NULL for the strictly linear tendency */
+  const void *u0, *v0;
+  /* inputs: adjoints of fu fv ke gt xu xv g yu yv (3-D) and gt_pi (2-D) */
+  const void *a_fu, *a_fv, *a_ke, *a_gt, *a_xu, *a_xv, *a_g, *a_yu, *a_yv, *a_gt_pi;
+  /* outputs: adjoints of u v t q vor div (3-D), pi_x pi_y (2-D) */
+  void *a_u, *a_v, *a_t, *a_q, *a_vor, *a_div, *a_pix, *a_piy;
+} lbm_tend_adj_args;
+
+/* Replaces: no reference function (the reference has no adjoint); transpose
+ * of the grid-point part of Dynamics.tendencies, dynamics.py:176-267. */
+int lbm_tendency_grid_adjoint(int prec, const lbm_tend_adj_args* a, void* stream);
+
+typedef struct lbm_implicit_adj_args {
+  int nmem, nmax, kmax;
+  double dt;
+  const void *lap, *kv, *kd, *ktt, *kq, *ww, *tmtx, *gg, *dsig, *minv;
+  const void *vd_vor, *vd_div, *vd_t, *vd_q;
+  /* inputs: adjoint of the new level */
+  const void *an_vor, *an_div, *an_t, *an_pi, *an_q;
+  /* outputs: adjoints of the previous level and of the explicit tendencies */
+  void *ap_vor, *ap_div, *ap_t, *ap_pi, *ap_q;
+  void *aw_vor, *aw_div, *aw_t, *aw_pi, *aw_q;
+} lbm_implicit_adj_args;
+
+/* Transpose of Integrator.step, integrator.py:264-315. */
+int lbm_implicit_step_adjoint(int prec, const lbm_implicit_adj_args* a, void* stream);
 
 /* ============================================================================
  * Fused ensemble stepper (the hot path).  The prognostic state lives in

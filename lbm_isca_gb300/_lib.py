@@ -35,7 +35,18 @@ class TendGridArgs(C.Structure):
                 + [("frc_t_stride", C.c_int64), ("frc_ps_stride", C.c_int64),
                    ("frc_q_stride", C.c_int64)]
                 + [(n, VP) for n in ("fu", "fv", "ke", "gt", "xu", "xv", "g", "yu", "yv",
-                                     "gt_pi", "omega", "sdot")])
+                                     "gt_pi", "omega", "sdot", "lin_u", "lin_v")])
+
+
+class TendAdjArgs(C.Structure):
+    _fields_ = ([("nmem", I32), ("nlat", I32), ("nlon", I32), ("kmax", I32),
+                 ("kappa", F64), ("epsvt", F64), ("rair", F64)]
+                + [(n, VP) for n in ("dsig", "sigm", "alpha", "w3", "wP", "cpg", "ww", "tmtx",
+                                     "tref", "ub", "vb", "tb", "qb", "tvb", "absvor", "divb",
+                                     "x5b", "sdotb", "pixb", "piyb", "u0", "v0", "a_fu", "a_fv",
+                                     "a_ke", "a_gt", "a_xu", "a_xv", "a_g", "a_yu", "a_yv",
+                                     "a_gt_pi", "a_u", "a_v", "a_t", "a_q", "a_vor", "a_div",
+                                     "a_pix", "a_piy")])
 
 
 class ImplicitArgs(C.Structure):
@@ -45,6 +56,15 @@ class ImplicitArgs(C.Structure):
                                      "p_vor", "p_div", "p_t", "p_pi", "p_q", "w_vor", "w_div",
                                      "w_t", "w_pi", "w_q", "n_vor", "n_div", "n_t", "n_pi",
                                      "n_q")])
+
+
+class ImplicitAdjArgs(C.Structure):
+    _fields_ = ([("nmem", I32), ("nmax", I32), ("kmax", I32), ("dt", F64)]
+                + [(n, VP) for n in ("lap", "kv", "kd", "ktt", "kq", "ww", "tmtx", "gg",
+                                     "dsig", "minv", "vd_vor", "vd_div", "vd_t", "vd_q",
+                                     "an_vor", "an_div", "an_t", "an_pi", "an_q", "ap_vor",
+                                     "ap_div", "ap_t", "ap_pi", "ap_q", "aw_vor", "aw_div",
+                                     "aw_t", "aw_pi", "aw_q")])
 
 
 class StepperDesc(C.Structure):
@@ -79,6 +99,8 @@ _SIGS = {
                                      VP, F64, VP, VP]),
     "lbm_tendency_grid": (I32, [I32, C.POINTER(TendGridArgs), VP]),
     "lbm_implicit_step": (I32, [I32, C.POINTER(ImplicitArgs), VP]),
+    "lbm_tendency_grid_adjoint": (I32, [I32, C.POINTER(TendAdjArgs), VP]),
+    "lbm_implicit_step_adjoint": (I32, [I32, C.POINTER(ImplicitAdjArgs), VP]),
     "lbm_stepper_prime": (I32, [C.POINTER(StepperDesc), VP]),
     "lbm_stepper_run": (I32, [C.POINTER(StepperDesc), C.POINTER(StepCtl), I32, VP]),
     "lbm_stepper_launch": (I32, [C.POINTER(StepperDesc), C.POINTER(StepCtl), I32, VP]),

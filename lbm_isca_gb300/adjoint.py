@@ -1,0 +1,506 @@
+"""Hand-written adjoint of the time step, with binomial checkpointing.
+
+The reference has no adjoint.  This module differentiates the reference's
+own step sequence (model.py:232-243):
+
+    tend = Dynamics.tendencies(ga, frc_t)         (dynamics.py:156-271)
+    prev = gb.to_spectral()                       (state.py:86-92)
+    new  = Integrator.step(dt, prev, tend)        (integrator.py:264-315)
+    gc   = load_spectral(new)                     (state.py:94-99)
+    gb'  = ga (start) | RA(gb, ga, gc)            (state.py:110-128)
+    ga'  = gc
+
+It is linear about the basic state except the kinetic energy
+0.5 (u^2 + v^2) of the tendency and the exact pi' <-> ps' conversions
+(pi' = ln(ps_bar + ps') - ln(ps_bar), ps' = ps_bar (e^pi' - 1)); those are
+linearised about the stored trajectory.
+
+Pieces, all on the device:
+* ``AdjointTransforms``: the transpose of every spectral operator of the
+  step.  Each is the library's opposite transform with rescaled tables:
+  the transpose of the inverse longitude transform is c_m I times the
+  forward one (c_0 = 1, c_m = 2), the transpose of the forward one is
+  h_m / I times the inverse one (h_0 = 1, h_m = 1/2), and the transpose of
+  a Legendre contraction with i m is the other contraction with -i m.
+* ``lbm_tendency_grid_adjoint`` / ``lbm_implicit_step_adjoint``: the grid
+  columns and the spectral coefficients (adjoint.cu).
+* ``TimeStep``: the step, its tangent-linear model and its adjoint, on grid
+  states (``State``), functional (inputs are never modified).
+* ``ForcingGradient``: the gradient of a scalar response of the final state
+  with respect to a steady 3-D heating (the ``frc_t`` argument), by a
+  forward sweep that stores at most ``snaps`` states on a binomial
+  schedule (``checkpoint.schedule``) and a reverse sweep that re-advances
+  from them.  ``HeatingResponse`` wraps it as a ``torch.autograd.Function``.
+"""
+
+from __future__ import annotations
+
+import types
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import ImplicitAdjArgs, TendAdjArgs, check, lib, ptr
+from .backend import stream_handle, to_device
+from .checkpoint import schedule as binomial_schedule
+from .configs import response_box
+from .constants import EPSVT, KAPPA, RAIR
+from .state import State
+
+FIELDS = ("u", "v", "t", "q", "ps")
+
+
+def _zeros_like_state(st):
+    return types.SimpleNamespace(**{k: torch.zeros_like(getattr(st, k)) for k in FIELDS})
+
+
+def _ns(**kw):
+    return types.SimpleNamespace(**kw)
+
+
+def state_dot(a, b):
+    """Euclidean inner product of two grid states (u v t q ps)."""
+    return sum(float((getattr(a, k) * getattr(b, k)).sum()) for k in FIELDS)
+
+
+def spec_dot(a, b):
+    """Real inner product of complex spectral arrays: sum Re(conj(a) b)."""
+    return float((a.conj() * b).real.sum())
+
+
+# ---------------------------------------------------------------------------
+# Transposed spectral operators
+# ---------------------------------------------------------------------------
+class AdjointTransforms:
+    """Transposes of the operators of ``Spectral`` (spectral.py:159-276)
+    under the Euclidean inner products of grid values and of (Re, Im)
+    spectral coefficients."""
+
+    def __init__(self, sp):
+        if sp.precision != "fp64":
+            raise ValueError("the adjoint runs in FP64")
+        self.sp = sp
+        M, I = sp.nmax + 1, sp.nlon
+        dev = sp.device
+        cm = torch.full((M,), 2.0 * I, dtype=torch.float64, device=dev)
+        cm[0] = float(I)
+        hm = torch.full((M,), 0.5 / I, dtype=torch.float64, device=dev)
+        hm[0] = 1.0 / I
+        t = sp._t
+        self.Pc = (t["P"] * cm[:, None, None]).contiguous()
+        self.Hc = (t["H"] * cm[:, None, None]).contiguous()
+        self.Pgw_h = (t["Pgw"] * hm[:, None, None]).contiguous()
+        self.Pgwdel_h = (t["Pgwdel"] * hm[:, None, None]).contiguous()
+        self.Hgwdel_h = (t["Hgwdel"] * hm[:, None, None]).contiguous()
+        self.neg_one = -torch.ones(M, dtype=torch.float64, device=dev)
+        self.neg_invlap = (-t["invlap"]).contiguous()
+        self.neg_cos = (-t["cos"]).contiguous()
+
+    def wave_to_grid_T(self, g):
+        sp = self.sp
+        g4, meta = sp._grid(g)
+        return sp._ret_spec(sp._anal(sp._fwd(g4), self.Pc, 0), meta)
+
+    def grid_to_wave_T(self, s):
+        sp = self.sp
+        s4, meta = sp._spec(s)
+        return sp._ret_grid(sp._inv(sp._synth(s4, self.Pgw_h, 0)), meta)
+
+    def hgrad_T(self, gx, gy):
+        sp = self.sp
+        x4, meta = sp._grid(gx)
+        y4, _ = sp._grid(gy)
+        rc = sp._t["rcos"]
+        s = sp._anal(sp._fwd(x4, rc), self.Pc, 1, sp._fwd(y4, rc), self.Hc, 0, -1.0,
+                     nfac=self.neg_one)
+        return sp._ret_spec(s, meta)
+
+    def uv_to_vordiv_T(self, vor, div):
+        sp = self.sp
+        v4, meta = sp._spec(vor)
+        d4, _ = sp._spec(div)
+        fv = sp._synth(v4, self.Pgwdel_h, 1, None, d4, self.Hgwdel_h, 0, None, 1.0)
+        fu = sp._synth(d4, self.Pgwdel_h, 1, None, v4, self.Hgwdel_h, 0, None, -1.0)
+        nc = self.neg_cos
+        return sp._ret_grid(sp._inv(fu, nc), meta), sp._ret_grid(sp._inv(fv, nc), meta)
+
+    def neg_divergence_T(self, s):
+        sp = self.sp
+        s4, meta = sp._spec(s)
+        c = sp._t["cos"]
+        fx = sp._inv(sp._synth(s4, self.Pgwdel_h, 1), c)
+        fy = sp._inv(sp._synth(s4, self.Hgwdel_h, 0), c)
+        return sp._ret_grid(fx, meta), sp._ret_grid(fy, meta)
+
+    def vordiv_to_uv_T(self, u, v):
+        sp = self.sp
+        u4, meta = sp._grid(u)
+        v4, _ = sp._grid(v)
+        rc = sp._t["rcos"]
+        fu, fv = sp._fwd(u4, rc), sp._fwd(v4, rc)
+        nil = self.neg_invlap
+        div = sp._anal(fu, self.Pc, 1, fv, self.Hc, 0, -1.0, nfac=nil)
+        vor = sp._anal(fv, self.Pc, 1, fu, self.Hc, 0, 1.0, nfac=nil)
+        return sp._ret_spec(vor, meta), sp._ret_spec(div, meta)
+
+
+# ---------------------------------------------------------------------------
+# The time step, its tangent-linear model and its adjoint
+# ---------------------------------------------------------------------------
+class TimeStep:
+    """One reference step on grid states of an ``LBM`` (FP64, one member)."""
+
+    def __init__(self, model):
+        if model.batched:
+            raise ValueError("the adjoint takes a single-member model")
+        self.m = model
+        self.sp, self.vg = model.sp, model.vg
+        self.tr = AdjointTransforms(model.sp)
+        self.ps_bar = model.ga.ps_bar
+        self.gamma = float(model.cfg.robert)
+        self.linear = bool(model.cfg.strictly_linear)
+
+    # ---- helpers ------------------------------------------------------------
+    def _state(self, u, v, t, q, ps):
+        return State(self.ps_bar, u=u, v=v, t=t, q=q, ps=ps, device=self.sp.device)
+
+    def zero_state(self):
+        J, I, K = self.sp.nlat, self.sp.nlon, self.vg.kmax
+        z3 = lambda: torch.zeros((J, I, K), dtype=torch.float64,   # noqa: E731
+                                 device=self.sp.device)
+        return self._state(z3(), z3(), z3(), z3(),
+                           torch.zeros((J, I), dtype=torch.float64, device=self.sp.device))
+
+    def _ra(self, prev, cur, nxt):
+        g = self.gamma
+        return self._state(*(getattr(cur, k) + g * (getattr(prev, k) - 2.0 * getattr(cur, k)
+                                                    + getattr(nxt, k)) for k in FIELDS))
+
+    # ---- forward ------------------------------------------------------------
+    def forward(self, ga, gb, dt, start, frc_t):
+        """(ga, gb) -> (ga', gb') for one call of the reference loop."""
+        m, sp = self.m, self.sp
+        tend = m.dyn.tendencies(ga, frc_t=frc_t)
+        new = m.integ.step(dt, gb.to_spectral(sp), tend)
+        gc = self.zero_state().load_spectral(sp, new)
+        gb_new = ga if start else self._ra(gb, ga, gc)
+        return gc, gb_new
+
+    # ---- tangent-linear -----------------------------------------------------
+    def _assemble(self, o, frc_vor=None, frc_div=None):
+        sp = self.sp
+        wt_pi = sp.grid_to_wave(o["gt_pi"])
+        wt_t = sp.neg_divergence(o["xu"], o["xv"]) + sp.grid_to_wave(o["gt"])
+        wt_vor, wt_div = sp.uv_to_vordiv(o["fu"], o["fv"])
+        wt_div = wt_div - sp.laplacian(sp.grid_to_wave(o["ke"]))
+        wt_q = sp.neg_divergence(o["yu"], o["yv"]) + sp.grid_to_wave(o["g"])
+        return wt_vor, wt_div, wt_t, wt_pi, wt_q
+
+    def tangent_tendencies(self, ga, dga, dfrc=None):
+        """Tangent-linear of Dynamics.tendencies about the grid state ga."""
+        sp = self.sp
+        vor_s, div_s = sp.uv_to_vordiv(dga.u, dga.v)
+        vor, div = sp.wave_to_grid(vor_s), sp.wave_to_grid(div_s)
+        dpi = dga.ps / (self.ps_bar + ga.ps)
+        pix, piy = sp.hgrad(sp.grid_to_wave(dpi))
+        lin = None if self.linear else (ga.u, ga.v)
+        o = self.m.dyn._grid_kernel(dga, vor, div, pix, piy, dfrc, None, None,
+                                    want_omega=False, lin=lin)
+        return self._assemble(o)
+
+    def tangent(self, ga, gb, gc_ps, dga, dgb, dt, start, dfrc=None):
+        """Tangent-linear step: (dga, dgb) -> (dga', dgb') about the trajectory
+        (ga, gb) whose next level has surface pressure gc_ps."""
+        sp = self.sp
+        tend = self.tangent_tendencies(ga, dga, dfrc)
+        vor, div = sp.uv_to_vordiv(dgb.u, dgb.v)
+        prev = {"vor": vor, "div": div, "t": sp.grid_to_wave(dgb.t),
+                "pi": sp.grid_to_wave(dgb.ps / (self.ps_bar + gb.ps)),
+                "q": sp.grid_to_wave(dgb.q)}
+        new = self.m.integ.step(dt, prev, tend)
+        u, v = sp.vordiv_to_uv(new["vor"], new["div"])
+        dgc = self._state(u, v, sp.wave_to_grid(new["t"]), sp.wave_to_grid(new["q"]),
+                          (self.ps_bar + gc_ps) * sp.wave_to_grid(new["pi"]))
+        dgb_new = dga if start else self._ra(dgb, dga, dgc)
+        return dgc, dgb_new
+
+    # ---- adjoint ------------------------------------------------------------
+    def _tend_adjoint_kernel(self, ga, a_o):
+        sp, vg, bs = self.sp, self.vg, self.m.bst
+        J, I, K = sp.nlat, sp.nlon, vg.kmax
+        f64 = dict(device=sp.device, dtype=torch.float64)
+        out = {k: torch.empty((J, I, K), **f64) for k in ("u", "v", "t", "q", "vor", "div")}
+        out["pix"] = torch.empty((J, I), **f64)
+        out["piy"] = torch.empty((J, I), **f64)
+        keep = []
+
+        def c(x):
+            t = x.contiguous()
+            keep.append(t)
+            return ptr(t)
+
+        a = TendAdjArgs()
+        a.nmem, a.nlat, a.nlon, a.kmax = 1, J, I, K
+        a.kappa, a.epsvt, a.rair = KAPPA, EPSVT, RAIR
+        a.dsig, a.sigm, a.alpha, a.w3, a.wP = (c(vg.dsig), c(vg.sigm), c(vg.alpha), c(vg.w3),
+                                               c(vg.wP))
+        a.cpg, a.ww, a.tmtx, a.tref = c(vg.cpg), c(vg.ww), c(vg.tmtx), c(vg.tbar)
+        a.ub, a.vb, a.tb, a.qb, a.tvb = c(bs.u), c(bs.v), c(bs.t), c(bs.q), c(bs.tv)
+        a.absvor, a.divb, a.x5b, a.sdotb = c(bs.absvor), c(bs.div), c(bs.x5), c(bs.sdot)
+        a.pixb, a.piyb = c(bs.pix), c(bs.piy)
+        if not self.linear:
+            a.u0, a.v0 = c(ga.u), c(ga.v)
+        for k in ("fu", "fv", "ke", "gt", "xu", "xv", "g", "yu", "yv", "gt_pi"):
+            setattr(a, "a_" + k, c(a_o[k]))
+        for k in ("u", "v", "t", "q", "vor", "div", "pix", "piy"):
+            setattr(a, "a_" + k, ptr(out[k]))
+        check(lib().lbm_tendency_grid_adjoint(_lib.LBM_F64, a, stream_handle()),
+              "lbm_tendency_grid_adjoint")
+        return out
+
+    def adjoint_tendencies(self, ga, aw):
+        """Transpose of ``tangent_tendencies``: adjoints of the five spectral
+        tendencies -> adjoint grid state (u v t q ps)."""
+        tr, sp = self.tr, self.sp
+        a_vor, a_div, a_t, a_pi, a_q = aw
+        a_o = {"gt_pi": tr.grid_to_wave_T(a_pi), "gt": tr.grid_to_wave_T(a_t),
+               "ke": tr.grid_to_wave_T(-sp.laplacian(a_div)), "g": tr.grid_to_wave_T(a_q)}
+        a_o["xu"], a_o["xv"] = tr.neg_divergence_T(a_t)
+        a_o["fu"], a_o["fv"] = tr.uv_to_vordiv_T(a_vor, a_div)
+        a_o["yu"], a_o["yv"] = tr.neg_divergence_T(a_q)
+        g = self._tend_adjoint_kernel(ga, a_o)
+        a_pis = tr.hgrad_T(g["pix"], g["piy"])
+        a_ps = tr.grid_to_wave_T(a_pis) / (self.ps_bar + ga.ps)
+        du, dv = tr.uv_to_vordiv_T(tr.wave_to_grid_T(g["vor"]), tr.wave_to_grid_T(g["div"]))
+        return _ns(u=g["u"] + du, v=g["v"] + dv, t=g["t"], q=g["q"], ps=a_ps)
+
+    def _implicit_adjoint(self, dt, an):
+        sp, vg = self.sp, self.vg
+        integ = self.m.integ
+        integ.semi.prepare(dt)
+        integ.vdiff.prepare(dt)
+        dmp = integ.dmp
+        keys = ("vor", "div", "t", "pi", "q")
+        an = {k: an[k].to(torch.complex128).contiguous() for k in keys}
+        ap = {k: torch.empty_like(an[k]) for k in keys}
+        aw = {k: torch.empty_like(an[k]) for k in keys}
+        keep = [vg.ww.contiguous(), vg.tmtx.contiguous(), vg.gg.contiguous(),
+                vg.dsig.contiguous()]
+        a = ImplicitAdjArgs()
+        a.nmem, a.nmax, a.kmax, a.dt = 1, sp.nmax, vg.kmax, float(dt)
+        a.lap, a.kv, a.kd, a.ktt, a.kq = (ptr(sp.laplace), ptr(dmp.kv), ptr(dmp.kd),
+                                          ptr(dmp.ktt), ptr(dmp.kq))
+        a.ww, a.tmtx, a.gg, a.dsig = (ptr(x) for x in keep)
+        a.minv = ptr(integ.semi.minv)
+        mv = integ.vdiff.minv
+        a.vd_vor, a.vd_div, a.vd_t, a.vd_q = (ptr(mv.get(n)) for n in ("vor", "div", "t", "q"))
+        a.an_vor, a.an_div, a.an_t, a.an_pi, a.an_q = (ptr(an[k]) for k in keys)
+        a.ap_vor, a.ap_div, a.ap_t, a.ap_pi, a.ap_q = (ptr(ap[k]) for k in keys)
+        a.aw_vor, a.aw_div, a.aw_t, a.aw_pi, a.aw_q = (ptr(aw[k]) for k in keys)
+        check(lib().lbm_implicit_step_adjoint(_lib.LBM_F64, a, stream_handle()),
+              "lbm_implicit_step_adjoint")
+        return ap, aw
+
+    def adjoint(self, ga, gb, gc_ps, a_ga, a_gb, dt, start):
+        """Transpose of ``tangent``: adjoints of (ga', gb') -> adjoints of
+        (ga, gb), plus the adjoint of the spectral T tendency (whose
+        grid-to-wave transpose is this step's heating gradient)."""
+        tr, g = self.tr, self.gamma
+        if start:
+            a_c = a_ga
+            a_a = a_gb
+            a_b = None
+        else:
+            a_c = _ns(**{k: getattr(a_ga, k) + g * getattr(a_gb, k) for k in FIELDS})
+            a_a = _ns(**{k: (1.0 - 2.0 * g) * getattr(a_gb, k) for k in FIELDS})
+            a_b = _ns(**{k: g * getattr(a_gb, k) for k in FIELDS})
+        # load_spectral
+        an_vor, an_div = tr.vordiv_to_uv_T(a_c.u, a_c.v)
+        an = {"vor": an_vor, "div": an_div, "t": tr.wave_to_grid_T(a_c.t),
+              "q": tr.wave_to_grid_T(a_c.q),
+              "pi": tr.wave_to_grid_T(a_c.ps * (self.ps_bar + gc_ps))}
+        ap, aw = self._implicit_adjoint(dt, an)
+        # to_spectral of gb
+        bu, bv = tr.uv_to_vordiv_T(ap["vor"], ap["div"])
+        b = _ns(u=bu, v=bv, t=tr.grid_to_wave_T(ap["t"]), q=tr.grid_to_wave_T(ap["q"]),
+                ps=tr.grid_to_wave_T(ap["pi"]) / (self.ps_bar + gb.ps))
+        if a_b is not None:
+            b = _ns(**{k: getattr(b, k) + getattr(a_b, k) for k in FIELDS})
+        # tendencies of ga
+        ta = self.adjoint_tendencies(ga, (aw["vor"], aw["div"], aw["t"], aw["pi"], aw["q"]))
+        a_prev = _ns(**{k: getattr(ta, k) + getattr(a_a, k) for k in FIELDS})
+        return a_prev, b, aw["t"]
+
+
+# ---------------------------------------------------------------------------
+# Response and gradient
+# ---------------------------------------------------------------------------
+class AreaMeanStreamfunction:
+    """Gaussian-weighted area mean of psi' = wave_to_grid(inv_laplacian(vor'))
+    at the full level nearest ``sigma`` over a latitude/longitude box
+    (bounds inclusive), from the final grid state's u, v."""
+
+    def __init__(self, sp, vg, sigma=0.25, lat=(30.0, 60.0), lon=(150.0, 210.0)):
+        self.sp = sp
+        sig = np.asarray(vg.host("sig"))
+        self.k = int(np.argmin(np.abs(sig - sigma)))
+        box = response_box(np.asarray(sp.lat_deg), np.asarray(sp.lon_deg), lat[0], lat[1],
+                           lon[0], lon[1])
+        self.npts = (int(box.any(axis=1).sum()), int(box.any(axis=0).sum()))
+        w = box * np.asarray(sp.gw)[:, None]
+        w = w / w.sum()
+        K = vg.kmax
+        wk = np.zeros((sp.nlat, sp.nlon, K))
+        wk[..., self.k] = w
+        self.weights = torch.as_tensor(wk, device=sp.device)
+
+    def __call__(self, st):
+        sp = self.sp
+        vor, _ = sp.uv_to_vordiv(st.u, st.v)
+        psi = sp.wave_to_grid(sp.inverse_laplacian(vor))
+        return (psi * self.weights).sum()
+
+    def seed(self, tr, like):
+        """Adjoint grid state of the response (d J / d final state)."""
+        sp = self.sp
+        a_vor = sp.inverse_laplacian(tr.wave_to_grid_T(self.weights))
+        u, v = tr.uv_to_vordiv_T(a_vor, torch.zeros_like(a_vor))
+        a = _zeros_like_state(like)
+        a.u, a.v = u, v
+        return a
+
+
+class ForcingGradient:
+    """J(heating) and dJ/d(heating) for a steady 3-D heating (K/s, the
+    ``frc_t`` argument of every call), from the model's zero initial state,
+    over the calls of ``LBM._schedule(nsteps)`` (start-up calls included).
+    The reverse sweep re-advances from at most ``snaps`` stored states."""
+
+    def __init__(self, model, response, nsteps=None, ndays=None, snaps=32):
+        self.step = TimeStep(model)
+        self.response = response
+        if nsteps is None:
+            nsteps = int(round((ndays if ndays is not None else model.cfg.ndays)
+                               * model.cfg.steps_per_day))
+        self.calls = model._schedule(nsteps)
+        self.snaps = int(snaps)
+        self.actions = binomial_schedule(len(self.calls), self.snaps)
+        self.forward_steps = 0
+        self.peak_stored = 0
+        self._saved = None
+
+    def _heating(self, heating):
+        sp, vg = self.step.sp, self.step.vg
+        h = to_device(heating, sp.device)
+        if tuple(h.shape) != (sp.nlat, sp.nlon, vg.kmax):
+            raise ValueError(f"heating must be (nlat, nlon, kmax) = "
+                             f"{(sp.nlat, sp.nlon, vg.kmax)}, got {tuple(h.shape)}")
+        return h.contiguous()
+
+    def _advance(self, cur, i, j, h):
+        for s in range(i, j):
+            dt, start = self.calls[s]
+            cur = self.step.forward(*cur, dt, start, h)
+            self.forward_steps += 1
+        return cur
+
+    def forward(self, heating):
+        """Forward sweep; returns J (0-d device tensor) and keeps the stored
+        states for ``backward``."""
+        h = self._heating(heating)
+        z = self.step.zero_state()
+        cur, pos, slots = (z, z), 0, {}
+        self.forward_steps, self.peak_stored = 0, 0
+        n = len(self.calls)
+        i = 0
+        acts = self.actions
+        while acts[i][0] != "adjoint":
+            cur, pos = self._do(acts[i], cur, pos, slots, h)
+            i += 1
+        # the last call: state n (the response); its ps' is the next level of
+        # call n - 1 in the reverse sweep
+        last = self._advance(cur, n - 1, n, h)
+        J = self.response(last[0])
+        self._saved = (h, i, cur, pos, slots, last[0].ps, last[0])
+        return J
+
+    def _do(self, act, cur, pos, slots, h):
+        kind = act[0]
+        if kind == "store":
+            slots[act[1]] = cur
+            self.peak_stored = max(self.peak_stored, len(slots))
+        elif kind == "restore":
+            cur, pos = slots[act[1]], act[1]
+        elif kind == "advance":
+            cur, pos = self._advance(cur, act[1], act[2], h), act[2]
+        elif kind == "free":
+            slots.pop(act[1])
+        return cur, pos
+
+    def backward(self):
+        """Reverse sweep; returns dJ/d(heating) on the grid."""
+        if self._saved is None:
+            raise RuntimeError("backward() needs a forward() first")
+        h, i, cur, pos, slots, next_ps, final = self._saved
+        st = self.step
+        a_ga = self.response.seed(st.tr, final)
+        a_gb = _zeros_like_state(final)
+        acc = None
+        for act in self.actions[i:]:
+            if act[0] != "adjoint":
+                cur, pos = self._do(act, cur, pos, slots, h)
+                continue
+            s = act[1]
+            if pos != s:
+                raise RuntimeError(f"checkpoint schedule out of step: at {pos}, reversing {s}")
+            dt, start = self.calls[s]
+            ga, gb = cur
+            a_ga, a_gb, a_wt = st.adjoint(ga, gb, next_ps, a_ga, a_gb, dt, start)
+            acc = a_wt.clone() if acc is None else acc + a_wt
+            next_ps = ga.ps
+            pos = None
+        self._saved = None
+        return st.tr.grid_to_wave_T(acc)
+
+    def value_and_grad(self, heating):
+        J = self.forward(heating)
+        return J, self.backward()
+
+    def tangent(self, heating, direction):
+        """Tangent-linear response dJ(heating; direction), the forward and the
+        tangent-linear model run side by side (the response is linear)."""
+        h, d = self._heating(heating), self._heating(direction)
+        st = self.step
+        z = st.zero_state()
+        cur, dcur = (z, z), (z, z)
+        for dt, start in self.calls:
+            nxt = st.forward(*cur, dt, start, h)
+            dcur = st.tangent(cur[0], cur[1], nxt[0].ps, *dcur, dt, start, dfrc=d)
+            cur = nxt
+        return self.response(dcur[0])
+
+    def value(self, heating):
+        """J alone, by a plain forward run (no stored states)."""
+        h = self._heating(heating)
+        z = self.step.zero_state()
+        cur = (z, z)
+        for dt, start in self.calls:
+            cur = self.step.forward(*cur, dt, start, h)
+        return self.response(cur[0])
+
+
+class HeatingResponse(torch.autograd.Function):
+    """``J = HeatingResponse.apply(heating, grad_driver)``; ``J.backward()``
+    runs the checkpointed adjoint and fills ``heating.grad``."""
+
+    @staticmethod
+    def forward(ctx, heating, driver):
+        ctx.driver = driver
+        with torch.no_grad():
+            return driver.forward(heating.detach())
+
+    @staticmethod
+    def backward(ctx, gJ):
+        g = ctx.driver.backward()
+        return gJ * g, None

@@ -96,7 +96,10 @@ __global__ void k_tendency_grid(lbm_tend_grid_args a) {
     R phiv = R(0);
     for (int l = 0; l < K; ++l) phiv += (x[l] - t[l]) * ww[k * K + l];
     R kek = phiv + u[k] * ub[k] + v[k] * vb[k];
-    if (!a.strictly_linear) kek += R(0.5) * (u[k] * u[k] + v[k] * v[k]);
+    if (a.lin_u)   // tangent-linear: linearised about the trajectory (lin_u, lin_v)
+      kek += P(a.lin_u)[p3 + k] * u[k] + P(a.lin_v)[p3 + k] * v[k];
+    else if (!a.strictly_linear)
+      kek += R(0.5) * (u[k] * u[k] + v[k] * v[k]);
     ke[k] = kek;
     // humidity (dynamics.py:256-262)
     yu[k] = u[k] * qb[k] + ub[k] * q[k];
@@ -199,6 +202,7 @@ extern "C" {
 int lbm_tendency_grid(int prec, const lbm_tend_grid_args* a, void* stream) {
   if (!a || a->nmem < 1 || a->kmax < 1 || a->kmax > KMAX_LOCAL || a->nlat < 2 || a->nlon < 2)
     return LBM_ERR_ARG;
+  if ((a->lin_u == nullptr) != (a->lin_v == nullptr)) return LBM_ERR_ARG;
   const size_t cols = (size_t)a->nmem * a->nlat * a->nlon;
   const int threads = 128;
   const unsigned blocks = (unsigned)((cols + threads - 1) / threads);

@@ -86,7 +86,10 @@ class Dynamics:
         self.strictly_linear = bool(strictly_linear)
         self.diag = {}
 
-    def _grid_kernel(self, st, vor, div, pix, piy, frc_t, frc_ps, frc_q, want_omega=True):
+    def _grid_kernel(self, st, vor, div, pix, piy, frc_t, frc_ps, frc_q, want_omega=True,
+                     lin=None):
+        """One launch of lbm_tendency_grid.  ``lin = (u0, v0)`` selects the
+        tangent-linear kinetic energy u0 u + v0 v in place of 0.5 (u^2 + v^2)."""
         sp, vg, bs = self.sp, self.vg, self.bs
         dev = sp.device
         u, v = st.u.contiguous(), st.v.contiguous()
@@ -135,6 +138,8 @@ class Dynamics:
         a.frc_q, a.frc_q_stride = frc(frc_q, shp3)
         for k in ("fu", "fv", "ke", "gt", "xu", "xv", "g", "yu", "yv", "gt_pi", "omega", "sdot"):
             setattr(a, k, ptr(out[k]))
+        if lin is not None:
+            a.lin_u, a.lin_v = c(lin[0]), c(lin[1])
         check(lib().lbm_tendency_grid(_lib.LBM_F64, a, stream_handle()), "lbm_tendency_grid")
         return out
 

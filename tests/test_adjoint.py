@@ -1,0 +1,390 @@
+"""Hand-written adjoint of the time step and the checkpointed forcing gradient.
+
+CPU tests: the binomial checkpoint schedule (consistency, stored-state
+limit, the binomial bound, which the recursion's exact minimum equals), and
+the column arithmetic of the adjoint kernels (adjoint_col.cuh built with
+g++) against a numpy restatement of the forward formulas
+(dynamics.py:176-267, integrator.py:264-315) by dot products.
+
+GPU tests (FP64): dot products of every transposed transform, of the
+tendency, implicit-update and whole-step adjoints against the tangent-linear
+model, the tangent-linear tendencies against the reference's own
+(``Dynamics(strictly_linear=True)``, golden fixture made by
+tests/golden/make_golden_adjoint.py) and the adjoint against it by a dot
+product, the whole-run tangent-linear response against the gradient, the
+gradient against central finite differences along 16 seeded directions
+(eps = 1e-4 relative), and checkpointing that changes nothing.
+"""
+
+import ctypes as C
+import os
+import shutil
+import subprocess
+import types
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden
+
+# ---------------------------------------------------------------- CPU tests
+
+
+def test_binomial_schedule_meets_the_bound():
+    from lbm_isca_gb300.checkpoint import binomial_cost, schedule, simulate
+
+    def exact(t, c, memo={}):
+        if t == 1:
+            return 0
+        if c == 1:
+            return t * (t - 1) // 2
+        key = (t, c)
+        if key not in memo:
+            memo[key] = min(l + exact(t - l, c - 1) + exact(l, c) for l in range(1, t))
+        return memo[key]
+
+    for t in range(1, 45):
+        for c in range(1, 7):
+            steps, peak, order = simulate(schedule(t, c))
+            assert order == list(range(t - 1, -1, -1))
+            assert peak <= c
+            assert steps == binomial_cost(t, min(c, t)) == exact(t, min(c, t))
+    # 20 days at dt = 1200 s (1440 steps + 2 start-up calls), 32 stored states
+    steps, peak, order = simulate(schedule(1442, 32))
+    assert peak == 32 and len(order) == 1442 and steps == binomial_cost(1442, 32) == 3731
+    with pytest.raises(ValueError):
+        schedule(0, 3)
+    with pytest.raises(ValueError):
+        simulate([("store", 0), ("advance", 1, 2)])
+
+
+@pytest.fixture(scope="module")
+def host_adjoint(tmp_path_factory):
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    out = str(tmp_path_factory.mktemp("adjcol") / "adjoint_col_host.so")
+    src = os.path.join(ROOT, "tests", "adjoint_col_host.cpp")
+    subprocess.check_call([gxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-o", out, src])
+    return C.CDLL(out)
+
+
+_D = C.POINTER(C.c_double)
+
+
+def _p(a):
+    return a.ctypes.data_as(_D) if a is not None else None
+
+
+def _parr(arrs):
+    return (_D * len(arrs))(*[_p(a) for a in arrs])
+
+
+def _column_forward(c, x):
+    """Tangent-linear grid-point tendency of one column (dynamics.py:176-267)."""
+    from oracle.lbm_oracle import column_sum, sigma_dot, vert_advect
+    u, v, t, q, vor, div, pix, piy = x
+    padv = u * c["pixb"] + c["ub"] * pix + v * c["piyb"] + c["vb"] * piy
+    S = column_sum(div + padv, c["dsig"])
+    sd = sigma_dot(S, c["sigm"])
+    tv = t + c["eps"] * (t * c["qb"] + c["tb"] * q)
+    x5 = c["alpha"] * div + c["wP"] * padv + c["w3"] * S[1:]
+    tdev, tvdev = c["tb"] - c["tref"], c["tvb"] - c["tref"]
+    rcpg = c["rair"] * c["cpg"]
+    va = lambda f, s: vert_advect(f, s, c["dsig"])   # noqa: E731
+    gt = (-c["kappa"] * (tv * c["x5b"] + c["tvb"] * x5) + t * c["divb"] + tdev * div
+          + va(t, c["sdb"]) + va(c["tb"], sd) + c["tmtx"] @ div)
+    fu = (v * c["absv"] + c["vb"] * vor - rcpg * (tv * c["pixb"] + tvdev * pix)
+          + va(u, c["sdb"]) + va(c["ub"], sd))
+    fv = (-u * c["absv"] - c["ub"] * vor - rcpg * (tv * c["piyb"] + tvdev * piy)
+          + va(v, c["sdb"]) + va(c["vb"], sd))
+    ke = c["ww"] @ (tv - t) + u * (c["ub"] + c["u0"]) + v * (c["vb"] + c["v0"])
+    return [fu, fv, ke, gt, u * tdev + c["ub"] * t, v * tdev + c["vb"] * t,
+            q * c["divb"] + c["qb"] * div + va(q, c["sdb"]) + va(c["qb"], sd),
+            u * c["qb"] + c["ub"] * q, v * c["qb"] + c["vb"] * q], -(padv * c["dsig"]).sum()
+
+
+def test_tendency_column_adjoint_is_the_transpose(host_adjoint):
+    rng = np.random.default_rng(3)
+    K = 7
+    r = lambda *s: rng.standard_normal(s)   # noqa: E731
+    sigm = np.concatenate([[1.0], np.sort(rng.uniform(0.05, 0.95, K - 1))[::-1], [0.0]])
+    sdb = np.concatenate([[0.0], r(K - 1), [0.0]])
+    c = dict(dsig=sigm[:-1] - sigm[1:], sigm=sigm, alpha=r(K), w3=r(K), wP=r(K), cpg=r(K),
+             ww=r(K, K), tmtx=r(K, K), tref=r(K), ub=r(K), vb=r(K), tb=r(K), qb=r(K),
+             tvb=r(K), absv=r(K), divb=r(K), x5b=r(K), sdb=sdb, pixb=0.3, piyb=-0.7,
+             kappa=0.2857, eps=0.608, rair=287.04, u0=r(K), v0=r(K))
+    x = [r(K) for _ in range(6)] + [0.4, -1.1]
+    y = [r(K) for _ in range(9)]
+    ypi = 0.9
+    out, gtpi = _column_forward(c, x)
+    lhs = sum(float(a @ b) for a, b in zip(out, y)) + gtpi * ypi
+    vert = [np.ascontiguousarray(c[k]) for k in ("dsig", "sigm", "alpha", "w3", "wP", "cpg",
+                                                 "ww", "tmtx", "tref")]
+    bs = [np.ascontiguousarray(c[k]) for k in ("ub", "vb", "tb", "qb", "tvb", "absv", "divb",
+                                               "x5b", "sdb")]
+    aout = [np.zeros(K) for _ in range(6)]
+    px, py = C.c_double(), C.c_double()
+    work = np.zeros(5 * (K + 1))
+    host_adjoint.host_tendency_column_adjoint(
+        C.c_int(K), C.c_double(c["kappa"]), C.c_double(c["eps"]), C.c_double(c["rair"]),
+        _parr(vert), _parr(bs), C.c_double(c["pixb"]), C.c_double(c["piyb"]), _p(c["u0"]),
+        _p(c["v0"]), _parr(y), C.c_double(ypi), _parr(aout), C.byref(px), C.byref(py),
+        _p(work))
+    rhs = sum(float(a @ b) for a, b in zip(x[:6], aout)) + x[6] * px.value + x[7] * py.value
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+def _implicit_forward(c, p, w, n):
+    """Semi-implicit update of one coefficient (integrator.py:264-315), real."""
+    dt = c["dt"]
+    ft = 1.0 + 2.0 * dt * c["ktt"]
+    sx = p["t"] * (1.0 + dt * c["ktt"]) + dt * w["t"]
+    wdphiy = c["ww"] @ sx + (p["pi"] + dt * w["pi"]) * ft * c["gg"]
+    rhs = p["div"] * (1.0 + dt * c["kd"]) * ft + dt * (w["div"] * ft - c["lap"] * wdphiy)
+    dbar = c["minv"] @ rhs
+    wt2, wpi2 = w["t"] - c["tmtx"] @ dbar, w["pi"] - c["dsig"] @ dbar
+    out = {"vor": (p["vor"] + 2 * dt * w["vor"]) / (1 + 2 * dt * c["kv"]),
+           "div": 2 * dbar - p["div"], "t": (p["t"] + 2 * dt * wt2) / ft,
+           "q": (p["q"] + 2 * dt * w["q"]) / (1 + 2 * dt * c["kq"]),
+           "pi": p["pi"] + 2 * dt * wpi2}
+    for f, vd in zip(("vor", "div", "t", "q"), c["vd"]):
+        if vd is not None and not (f in ("vor", "div") and n < 2):
+            out[f] = vd @ out[f]
+    return out
+
+
+@pytest.mark.parametrize("n", [1, 5])
+def test_implicit_coefficient_adjoint_is_the_transpose(host_adjoint, n):
+    rng = np.random.default_rng(11 + n)
+    K = 6
+    r = lambda *s: rng.standard_normal(s)   # noqa: E731
+    c = dict(dt=1200.0, lap=-n * (n + 1) / 6.371e6 ** 2, kv=abs(r(K)) * 1e-5,
+             kd=abs(r(K)) * 1e-5, ktt=abs(r(K)) * 1e-5, kq=abs(r(K)) * 1e-5, ww=r(K, K),
+             tmtx=r(K, K), gg=r(K) * 1e4, dsig=abs(r(K)), minv=r(K, K),
+             vd=[r(K, K), r(K, K), None, r(K, K)])
+    fields = ("vor", "div", "t", "q")
+    p = {f: r(K) for f in fields}
+    w = {f: r(K) for f in fields}
+    p["pi"], w["pi"] = 0.3, -0.8
+    y = {f: r(K) for f in fields}
+    y["pi"] = 1.7
+    out = _implicit_forward(c, p, w, n)
+    lhs = sum(float(np.dot(out[f], y[f])) for f in fields) + out["pi"] * y["pi"]
+    ops = [np.ascontiguousarray(c[k]) for k in ("kv", "kd", "ktt", "kq", "ww", "tmtx", "gg",
+                                                "dsig", "minv")]
+    ap, aw = [np.zeros(K) for _ in fields], [np.zeros(K) for _ in fields]
+    app, awp = C.c_double(), C.c_double()
+    host_adjoint.host_implicit_coef_adjoint(
+        C.c_int(K), C.c_double(c["dt"]), C.c_double(c["lap"]), _parr(ops), _parr(c["vd"]),
+        C.c_int(int(n < 2)), _parr([y[f] for f in fields]), C.c_double(y["pi"]), _parr(ap),
+        C.byref(app), _parr(aw), C.byref(awp), _p(np.zeros(4 * K)))
+    rhs = (sum(float(np.dot(p[f], a)) + float(np.dot(w[f], b)) for f, a, b in
+               zip(fields, ap, aw)) + p["pi"] * app.value + w["pi"] * awp.value)
+    assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), 1.0)
+
+
+# ---------------------------------------------------------------- GPU tests
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _model(K=20, strictly_linear=False, **extra):
+    from lbm_isca_gb300 import LBM, Config, Spectral, VerticalGrid, configs
+    sigm = configs.equal_sigma_half_levels(K)
+    bs = configs.solid_body_basic_state(64, 32, sigm)
+    sp = Spectral(nlon=64, nlat=32, nmax=21)
+    vg = VerticalGrid(sigm=sigm)
+    kw = dict(configs.plain_damping(K), strictly_linear=strictly_linear)
+    kw.update(extra)
+    cfg = Config(ndays=1.0, **kw)
+    return LBM(bs, sp, vg, cfg), sigm
+
+
+class _Rand:
+    def __init__(self, torch, seed, M=22, J=32, I=64, K=20):
+        self.t, self.rng, self.M, self.J, self.I, self.K = torch, np.random.default_rng(seed), M, J, I, K
+
+    def grid(self, k=True, scale=1.0):
+        shape = (self.J, self.I, self.K) if k else (self.J, self.I)
+        return self.t.as_tensor(scale * self.rng.standard_normal(shape)).cuda()
+
+    def spec(self, k=True):
+        M = self.M
+        shape = (M, M, self.K) if k else (M, M)
+        x = self.rng.standard_normal(shape) + 1j * self.rng.standard_normal(shape)
+        mask = np.triu(np.ones((M, M), bool))
+        return self.t.as_tensor(np.where(mask[..., None] if k else mask, x, 0)).cuda()
+
+    def state(self, step, ps_scale=1.0):
+        return step._state(self.grid(), self.grid(), self.grid(), self.grid(scale=1e-3),
+                           self.grid(False, ps_scale))
+
+
+def _rel(a, b):
+    return abs(a - b) / max(abs(a), abs(b))
+
+
+@pytest.mark.gpu
+def test_transposed_transforms_dot_products(torch_cuda):
+    from lbm_isca_gb300.adjoint import AdjointTransforms, spec_dot
+    m, _ = _model()
+    sp, tr, r = m.sp, AdjointTransforms(m.sp), _Rand(torch_cuda, 1)
+    gd = lambda a, b: float((a * b).sum())   # noqa: E731
+    for k in (True, False):
+        x, y = r.spec(k), r.grid(k)
+        assert _rel(gd(sp.wave_to_grid(x), y), spec_dot(x, tr.wave_to_grid_T(y))) < 1e-13
+        g, s = r.grid(k), r.spec(k)
+        assert _rel(spec_dot(sp.grid_to_wave(g), s), gd(g, tr.grid_to_wave_T(s))) < 1e-13
+    x, gx, gy = r.spec(), r.grid(), r.grid()
+    hx, hy = sp.hgrad(x)
+    assert _rel(gd(hx, gx) + gd(hy, gy), spec_dot(x, tr.hgrad_T(gx, gy))) < 1e-13
+    u, v, s1, s2 = r.grid(), r.grid(), r.spec(), r.spec()
+    vo, di = sp.uv_to_vordiv(u, v)
+    au, av = tr.uv_to_vordiv_T(s1, s2)
+    assert _rel(spec_dot(vo, s1) + spec_dot(di, s2), gd(u, au) + gd(v, av)) < 1e-13
+    fx, fy = tr.neg_divergence_T(s1)
+    assert _rel(spec_dot(sp.neg_divergence(u, v), s1), gd(u, fx) + gd(v, fy)) < 1e-13
+    uu, vv = sp.vordiv_to_uv(s1, s2)
+    a1, a2 = tr.vordiv_to_uv_T(u, v)
+    assert _rel(gd(uu, u) + gd(vv, v), spec_dot(s1, a1) + spec_dot(s2, a2)) < 1e-13
+
+
+@pytest.mark.gpu
+def test_tendency_and_implicit_adjoints_dot_products(torch_cuda):
+    from lbm_isca_gb300.adjoint import TimeStep, spec_dot, state_dot
+    m, _ = _model(vdifv=1.0e3, vdifd=1.0e3, vdift=1.0e3, vdifq=2.0e3)
+    st, r = TimeStep(m), _Rand(torch_cuda, 2)
+    ga, dx = r.state(st), r.state(st)
+    aw = [r.spec(), r.spec(), r.spec(), r.spec(False), r.spec()]
+    lhs = sum(spec_dot(a, b) for a, b in zip(st.tangent_tendencies(ga, dx), aw))
+    assert _rel(lhs, state_dot(dx, st.adjoint_tendencies(ga, aw))) < 1e-12
+    keys = ("vor", "div", "t", "pi", "q")
+    for dt in (300.0, 1200.0):
+        p = {k: r.spec(k != "pi") for k in keys}
+        w = [r.spec(k != "pi") for k in keys]
+        y = {k: r.spec(k != "pi") for k in keys}
+        new = m.integ.step(dt, p, w)
+        ap, aw2 = st._implicit_adjoint(dt, y)
+        lhs = sum(spec_dot(new[k], y[k]) for k in keys)
+        rhs = (sum(spec_dot(p[k], ap[k]) for k in keys)
+               + sum(spec_dot(wi, aw2[k]) for wi, k in zip(w, keys)))
+        assert _rel(lhs, rhs) < 1e-12
+
+
+@pytest.mark.gpu
+def test_step_adjoint_dot_product_and_taylor(torch_cuda):
+    """Whole step: <TL dx, y> = <dx, ADJ y> to 1e-10 (start-up and leapfrog
+    calls), and the TL is the derivative of the nonlinear step."""
+    from lbm_isca_gb300.adjoint import FIELDS, TimeStep, state_dot
+    m, _ = _model()
+    st, r = TimeStep(m), _Rand(torch_cuda, 3)
+    ga, gb = r.state(st, 5.0), r.state(st, 5.0)
+    dga, dgb = r.state(st), r.state(st)
+    for start, dt in ((True, 300.0), (False, 1200.0)):
+        gc, _ = st.forward(ga, gb, dt, start, None)
+        t1, t2 = st.tangent(ga, gb, gc.ps, dga, dgb, dt, start)
+        y1, y2 = r.state(st), r.state(st)
+        lhs = state_dot(t1, y1) + state_dot(t2, y2)
+        a1, a2, _ = st.adjoint(ga, gb, gc.ps, y1, y2, dt, start)
+        assert _rel(lhs, state_dot(dga, a1) + state_dot(dgb, a2)) < 1e-10
+        eps = 1e-3
+        sh = lambda s, d, e: st._state(*(getattr(s, k) + e * getattr(d, k)   # noqa: E731
+                                         for k in FIELDS))
+        c1, _ = st.forward(sh(ga, dga, eps), sh(gb, dgb, eps), dt, start, None)
+        c2, _ = st.forward(sh(ga, dga, -eps), sh(gb, dgb, -eps), dt, start, None)
+        num = sum(float(((getattr(c1, k) - getattr(c2, k)) / (2 * eps)
+                         - getattr(t1, k)).abs().max()) for k in FIELDS)
+        assert num / sum(float(getattr(t1, k).abs().max()) for k in FIELDS) < 1e-8
+
+
+@pytest.mark.gpu
+def test_adjoint_against_reference_tangent_linear(torch_cuda):
+    """The reference's own tangent-linear tendencies (strictly linear
+    Dynamics on its synthetic jet and test direction, T21, 5 layers):
+    ours reproduce them, and the adjoint is their transpose."""
+    from lbm_isca_gb300 import LBM, Config, Spectral, VerticalGrid
+    from lbm_isca_gb300.adjoint import TimeStep, state_dot
+    torch = torch_cuda
+    g = golden("adjoint_tl.npz")
+    J, I, K = 32, 64, 5
+    z3 = lambda p: np.broadcast_to(p[:, None, :], (J, I, K)).copy()   # noqa: E731
+    bs = types.SimpleNamespace(u=z3(g["bs_u"]), v=np.zeros((J, I, K)), t=z3(g["bs_t"]),
+                               q=z3(g["bs_q"]), ps=np.full((J, I), float(g["bs_ps"])))
+    sp, vg = Spectral(nlon=64, nlat=32, nmax=21), VerticalGrid(sigm=g["sigm"])
+    m = LBM(bs, sp, vg, Config(strictly_linear=True, sponge=False, ddragv=None, ddragd=None,
+                               ddragt=None))
+    st = TimeStep(m)
+    T = lambda a: torch.as_tensor(np.asarray(a)).cuda()   # noqa: E731
+    zero = st.zero_state()
+    dx = st._state(T(g["u0"]), T(g["v0"]), T(g["t0"]), T(g["q0"]),
+                   T(float(g["bs_ps"]) * g["pi0"]))
+    names = ("vor", "div", "t", "pi", "q")
+    for n, x in zip(names, st.tangent_tendencies(zero, dx)):
+        ref = g["L_" + n]
+        assert np.abs(x.cpu().numpy() - ref).max() <= 1e-10 * np.abs(ref).max(), n
+    r = _Rand(torch, 7, K=K)
+    ys = [r.spec(n != "pi") for n in names]
+    lhs = sum(float((np.conj(g["L_" + n]) * y.cpu().numpy()).real.sum())
+              for n, y in zip(names, ys))
+    rhs = state_dot(dx, st.adjoint_tendencies(zero, ys))
+    assert abs(lhs - rhs) <= 1e-10 * abs(lhs)
+
+
+@pytest.fixture(scope="module")
+def gradient_case(torch_cuda):
+    from lbm_isca_gb300 import configs
+    from lbm_isca_gb300.adjoint import AreaMeanStreamfunction, ForcingGradient
+    m, sigm = _model()
+    resp = AreaMeanStreamfunction(m.sp, m.vg)
+    assert resp.npts == (6, 11)
+    heat = torch_cuda.as_tensor(configs.elliptic_heating(64, 32, sigm)).cuda()
+    fg = ForcingGradient(m, resp, nsteps=36, snaps=6)
+    J, grad = fg.value_and_grad(heat)
+    return types.SimpleNamespace(m=m, resp=resp, heat=heat, fg=fg, J=float(J), grad=grad)
+
+
+@pytest.mark.gpu
+def test_gradient_tangent_linear_run_dot_product(gradient_case, torch_cuda):
+    c = gradient_case
+    r = _Rand(torch_cuda, 21)
+    for _ in range(2):
+        d = r.grid() * float(c.heat.abs().max())
+        tl = float(c.fg.tangent(c.heat, d))
+        assert _rel(tl, float((c.grad * d).sum())) < 1e-10
+
+
+@pytest.mark.gpu
+def test_gradient_matches_central_differences(gradient_case, torch_cuda):
+    """16 seeded random directions, eps = 1e-4 relative to the heating."""
+    c = gradient_case
+    assert abs(c.J - float(c.fg.value(c.heat))) <= 1e-12 * abs(c.J)
+    rng = np.random.default_rng(16)
+    hmax = float(c.heat.abs().max())
+    worst = 0.0
+    for _ in range(16):
+        d = torch_cuda.as_tensor(rng.standard_normal(tuple(c.heat.shape))).cuda() * hmax
+        eps = 1e-4
+        fd = (float(c.fg.value(c.heat + eps * d)) - float(c.fg.value(c.heat - eps * d))) / (2 * eps)
+        worst = max(worst, _rel(fd, float((c.grad * d).sum())))
+    assert worst < 1e-6
+
+
+@pytest.mark.gpu
+def test_checkpointing_changes_nothing(gradient_case, torch_cuda):
+    from lbm_isca_gb300.adjoint import ForcingGradient, HeatingResponse
+    c = gradient_case
+    assert c.fg.peak_stored <= 6
+    full = ForcingGradient(c.m, c.resp, nsteps=36, snaps=64)
+    J2, g2 = full.value_and_grad(c.heat)
+    assert float(J2) == c.J and bool((g2 == c.grad).all())
+    assert full.forward_steps == len(full.calls)       # every state stored: no re-steps
+    h = c.heat.clone().requires_grad_(True)
+    HeatingResponse.apply(h, ForcingGradient(c.m, c.resp, nsteps=36, snaps=3)).backward()
+    assert bool((h.grad == c.grad).all())
