@@ -50,6 +50,11 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the accuracy / plain-FP64 / CPU side measurements")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="checkpointed-adjoint cost and accuracy (T42L20, 20 days, FP64, "
+                         "32 stored states) instead of the bench")
+    ap.add_argument("--fd-dirs", type=int, default=4,
+                    help="central-difference directions checked by --adjoint")
     ap.add_argument("--sweep", action="store_true",
                     help="precision sweep (FP32 vs FP64 per field at days 10 and 30, "
                          "T42L20 x 128 members and T85L40 x 16 members) instead of the bench")
@@ -308,8 +313,86 @@ def precision_sweep(torch):
     return out
 
 
+def adjoint_measurement(torch, days=20.0, snaps=32, fd_dirs=4):
+    """Gradient of the area-mean day-20 streamfunction at sigma 0.25 over
+    30-60N 150-210E with respect to the 20 x 64 x 128 heating (solid-body
+    basic state, elliptic heating, plain damping, T42L20, FP64), by the
+    checkpointed adjoint; its time against the forward run of the same step
+    (graph-replayed reference-layout calls) and against the fused FP64
+    stepper's run, and central differences (eps 1e-4 relative) along seeded
+    directions."""
+    import types as _t
+    from lbm_isca_gb300 import LBM, Config, Spectral, VerticalGrid, configs
+    from lbm_isca_gb300.adjoint import AreaMeanStreamfunction, ForcingGradient
+    K = K_LEV
+    sigm = configs.equal_sigma_half_levels(K)
+    bs = configs.solid_body_basic_state(128, 64, sigm)
+    heat = torch.as_tensor(configs.elliptic_heating(128, 64, sigm), device="cuda")
+    sp, vg = Spectral(), VerticalGrid(sigm=sigm)
+    mk = lambda nd, **kw: LBM(bs, sp, vg, Config(ndays=nd, **dict(configs.plain_damping(K),  # noqa
+                                                                   **kw)))
+    model = mk(days)
+    resp = AreaMeanStreamfunction(sp, vg)
+    warm = ForcingGradient(model, resp, nsteps=4, snaps=2)
+    warm.value_and_grad(heat)                        # captures every graph variant
+    fg = ForcingGradient(model, resp, ndays=days, snaps=snaps)
+    fg._fg, fg._ag = warm._fg, warm._ag
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    J_fwd, t_fwd = timed(lambda: fg.value(heat))
+    (J, grad), t_grad = timed(lambda: fg.value_and_grad(heat))
+    seq = ForcingGradient(model, resp, ndays=days, snaps=snaps, pipeline=False)
+    seq._fg, seq._ag = warm._fg, warm._ag
+    (_, grad_seq), t_seq = timed(lambda: seq.value_and_grad(heat))
+    sf = _t.SimpleNamespace(t=heat, vor=None, div=None, ps=None)
+    m2 = mk(1.0, precision="fp64")
+    m2.run(steady_forcing=sf, verbose=False)          # warm-up (graph capture)
+    m2.cfg.ndays = days
+    _, t_fused = timed(lambda: m2.run(steady_forcing=sf, verbose=False))
+    m3 = mk(days, precision="fp64")
+    m3.run(steady_forcing=sf, verbose=False)
+    J_fused = float(resp(m3.ga))
+    rng = np.random.default_rng(16)
+    hmax = float(heat.abs().max())
+    fd = []
+    for _ in range(fd_dirs):
+        d = torch.as_tensor(rng.standard_normal(tuple(heat.shape)), device="cuda") * hmax
+        e = 1e-4
+        num = (float(fg.value(heat + e * d)) - float(fg.value(heat - e * d))) / (2 * e)
+        adj = float((grad * d).sum())
+        fd.append(abs(num - adj) / abs(num))
+    calls = len(fg.calls)
+    return {
+        "workload": "T42L20 solid-body basic state, elliptic heating (0N 120E), plain damping, "
+                    "FP64, 20 days (1440 steps + 2 start-up calls); response: area-mean psi' "
+                    "at sigma 0.25, 30-60N x 150-210E, day 20",
+        "J": float(J), "J_forward_run": float(J_fwd), "J_fused_fp64_run": J_fused,
+        "snaps": snaps, "peak_stored_states": fg.peak_stored, "calls": calls,
+        "forward_steps_in_gradient": fg.forward_steps,
+        "forward_s": t_fwd, "gradient_s": t_grad, "gradient_over_forward": t_grad / t_fwd,
+        "gradient_one_stream_s": t_seq,
+        "one_stream_vs_two_max_rel_diff": float((grad_seq - grad).abs().max()
+                                                / grad.abs().max()),
+        "fused_fp64_forward_s": t_fused, "gradient_over_fused_forward": t_grad / t_fused,
+        "fd_rel_err": fd, "fd_max_rel_err": max(fd) if fd else None,
+        "grad_absmax": float(grad.abs().max()),
+    }
+
+
 def main():
     args = parse()
+    if args.adjoint:
+        import torch
+        torch.cuda.set_device(0)
+        out = adjoint_measurement(torch, fd_dirs=args.fd_dirs)
+        print(json.dumps({"adjoint": out}), flush=True)
+        return
     if args.sweep:
         import torch
         torch.cuda.set_device(0)

@@ -158,12 +158,42 @@ class TimeStep:
         self.sp, self.vg = model.sp, model.vg
         self.tr = AdjointTransforms(model.sp)
         self.ps_bar = model.ga.ps_bar
+        self.lnps_bar = model.ga.lnps_bar
         self.gamma = float(model.cfg.robert)
         self.linear = bool(model.cfg.strictly_linear)
 
     # ---- helpers ------------------------------------------------------------
+    def resources(self):
+        """Every device tensor of the model the step reads (tables, basic
+        state, operators, matrices).  A captured CUDA graph holds these so
+        that its baked-in pointers stay valid even if the model replaces an
+        attribute later (a second LBM on the same VerticalGrid resets its
+        reference-temperature operators)."""
+        m = self.m
+        objs = [self.sp, self.sp._t, self.vg, m.bst, m.damping, m.integ.semi,
+                m.integ.semi._cache, m.integ.vdiff.minv, m.integ.vdiff._cache, self.tr,
+                {"ps_bar": self.ps_bar, "lnps_bar": self.lnps_bar}]
+        out, seen = [], set()
+
+        def grab(x, depth):
+            if isinstance(x, torch.Tensor):
+                if id(x) not in seen:
+                    seen.add(id(x))
+                    out.append(x)
+            elif depth > 0 and isinstance(x, (dict, list, tuple)):
+                for v in (x.values() if isinstance(x, dict) else x):
+                    grab(v, depth - 1)
+
+        for o in objs:
+            grab(o if isinstance(o, dict) else vars(o), 3)
+        return out
+
     def _state(self, u, v, t, q, ps):
-        return State(self.ps_bar, u=u, v=v, t=t, q=q, ps=ps, device=self.sp.device)
+        st = State.__new__(State)           # fields given: skip the constructor's setup
+        st.xp, st.device = torch, self.sp.device
+        st.ps_bar, st.lnps_bar = self.ps_bar, self.lnps_bar
+        st.u, st.v, st.t, st.q, st.ps = u, v, t, q, ps
+        return st
 
     def zero_state(self):
         J, I, K = self.sp.nlat, self.sp.nlon, self.vg.kmax
@@ -183,7 +213,9 @@ class TimeStep:
         m, sp = self.m, self.sp
         tend = m.dyn.tendencies(ga, frc_t=frc_t)
         new = m.integ.step(dt, gb.to_spectral(sp), tend)
-        gc = self.zero_state().load_spectral(sp, new)
+        u, v = sp.vordiv_to_uv(new["vor"], new["div"])
+        gc = self._state(u, v, sp.wave_to_grid(new["t"]), sp.wave_to_grid(new["q"]),
+                         self.ps_bar * (torch.exp(sp.wave_to_grid(new["pi"])) - 1.0))
         gb_new = ga if start else self._ra(gb, ga, gc)
         return gc, gb_new
 
@@ -371,14 +403,48 @@ class AreaMeanStreamfunction:
         return a
 
 
+class _GraphedCall:
+    """A function of flat device tensors captured once as a CUDA graph:
+    each call copies its arguments into the captured inputs and replays.
+    The outputs are the graph's own buffers, overwritten by the next replay."""
+
+    def __init__(self, fn, inputs, keep=()):
+        self.keep = list(keep)            # tensors whose addresses the graph holds
+        self.inputs = [x.clone() for x in inputs]
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            fn(*self.inputs)              # first use (lazy setup) outside the capture
+        torch.cuda.current_stream().wait_stream(side)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph, capture_error_mode="relaxed"):
+            self.outputs = fn(*self.inputs)
+
+    def __call__(self, *inputs):
+        torch._foreach_copy_(self.inputs, list(inputs))
+        self.graph.replay()
+        return self.outputs
+
+
+def _flat(*states):
+    return [getattr(st, k) for st in states for k in FIELDS]
+
+
 class ForcingGradient:
     """J(heating) and dJ/d(heating) for a steady 3-D heating (K/s, the
     ``frc_t`` argument of every call), from the model's zero initial state,
     over the calls of ``LBM._schedule(nsteps)`` (start-up calls included).
-    The reverse sweep re-advances from at most ``snaps`` stored states."""
+    The reverse sweep re-advances from at most ``snaps`` stored states.
+    With ``use_graph`` every forward call and every adjoint call replays a
+    CUDA graph of its (dt, start-up) variant; the kernels and their order
+    are those of the eager calls, so the results are bitwise the same."""
 
-    def __init__(self, model, response, nsteps=None, ndays=None, snaps=32):
+    def __init__(self, model, response, nsteps=None, ndays=None, snaps=32, use_graph=True,
+                 pipeline=True):
         self.step = TimeStep(model)
+        self.use_graph = bool(use_graph)
+        self.pipeline = bool(pipeline)
+        self._fg, self._ag = {}, {}
         self.response = response
         if nsteps is None:
             nsteps = int(round((ndays if ndays is not None else model.cfg.ndays)
@@ -398,10 +464,47 @@ class ForcingGradient:
                              f"{(sp.nlat, sp.nlon, vg.kmax)}, got {tuple(h.shape)}")
         return h.contiguous()
 
+    def _fwd_call(self, cur, s, h):
+        st = self.step
+        dt, start = self.calls[s]
+        if not self.use_graph:
+            return st.forward(*cur, dt, start, h)
+        g = self._fg.get((dt, start))
+        flat = _flat(*cur) + [h]
+        if g is None:
+            def fn(*x):
+                gc, gbn = st.forward(st._state(*x[0:5]), st._state(*x[5:10]), dt, start, x[10])
+                out = _flat(gc, gbn)
+                return [o.clone() if any(o is i for i in x) else o for o in out]
+            g = self._fg[(dt, start)] = _GraphedCall(fn, flat, st.resources())
+        out = g(*flat)
+        return st._state(*out[0:5]), st._state(*out[5:10])
+
+    def _adj_call(self, cur, next_ps, a_ga, a_gb, s):
+        st = self.step
+        dt, start = self.calls[s]
+        if not self.use_graph:
+            return st.adjoint(cur[0], cur[1], next_ps, a_ga, a_gb, dt, start)
+        g = self._ag.get((dt, start))
+        flat = _flat(*cur) + [next_ps] + _flat(a_ga, a_gb)
+        if g is None:
+            def fn(*x):
+                a, b, w = st.adjoint(st._state(*x[0:5]), st._state(*x[5:10]), x[10],
+                                     _ns(**dict(zip(FIELDS, x[11:16]))),
+                                     _ns(**dict(zip(FIELDS, x[16:21]))), dt, start)
+                return _flat(a, b) + [w]
+            g = self._ag[(dt, start)] = _GraphedCall(fn, flat, st.resources())
+        out = g(*flat)
+        return (_ns(**dict(zip(FIELDS, out[0:5]))), _ns(**dict(zip(FIELDS, out[5:10]))),
+                out[10])
+
+    def _own(self, st):
+        """A state that later graph replays cannot overwrite."""
+        return self.step._state(*(x.clone() for x in _flat(st))) if self.use_graph else st
+
     def _advance(self, cur, i, j, h):
         for s in range(i, j):
-            dt, start = self.calls[s]
-            cur = self.step.forward(*cur, dt, start, h)
+            cur = self._fwd_call(cur, s, h)
             self.forward_steps += 1
         return cur
 
@@ -420,14 +523,15 @@ class ForcingGradient:
             i += 1
         # the last call: state n (the response); its ps' is the next level of
         # call n - 1 in the reverse sweep
-        last = self._advance(cur, n - 1, n, h)
-        J = self.response(last[0])
-        self._saved = (h, i, cur, pos, slots, last[0].ps, last[0])
+        last = self._own(self._advance(cur, n - 1, n, h)[0])
+        J = self.response(last)
+        self._saved = (h, i, cur, pos, slots, last.ps, last)
         return J
 
     def _do(self, act, cur, pos, slots, h):
         kind = act[0]
         if kind == "store":
+            cur = (self._own(cur[0]), self._own(cur[1]))
             slots[act[1]] = cur
             self.peak_stored = max(self.peak_stored, len(slots))
         elif kind == "restore":
@@ -446,6 +550,10 @@ class ForcingGradient:
         st = self.step
         a_ga = self.response.seed(st.tr, final)
         a_gb = _zeros_like_state(final)
+        if self.use_graph and self.pipeline:
+            g = self._backward_pipelined(h, i, cur, pos, slots, next_ps, a_ga, a_gb)
+            self._saved = None
+            return g
         acc = None
         for act in self.actions[i:]:
             if act[0] != "adjoint":
@@ -454,13 +562,62 @@ class ForcingGradient:
             s = act[1]
             if pos != s:
                 raise RuntimeError(f"checkpoint schedule out of step: at {pos}, reversing {s}")
-            dt, start = self.calls[s]
-            ga, gb = cur
-            a_ga, a_gb, a_wt = st.adjoint(ga, gb, next_ps, a_ga, a_gb, dt, start)
+            a_ga, a_gb, a_wt = self._adj_call(cur, next_ps, a_ga, a_gb, s)
             acc = a_wt.clone() if acc is None else acc + a_wt
-            next_ps = ga.ps
+            next_ps = cur[0].ps.clone() if self.use_graph else cur[0].ps
             pos = None
         self._saved = None
+        return st.tr.grid_to_wave_T(acc)
+
+    def _backward_pipelined(self, h, i, cur, pos, slots, next_ps, a_ga, a_gb, depth=3):
+        """The reverse sweep on two streams.  The schedule's restore /
+        advance / store actions depend only on stored states, never on
+        adjoint results, so they run ahead on a second stream and hand each
+        state to be reversed through a ring of ``depth`` buffers; the adjoint
+        calls run on the current stream, each after an event for its state,
+        and each buffer is refilled only after an event that its adjoint call
+        has read it.  Both streams replay CUDA graphs; one member's kernels
+        leave most of the GPU idle, so the two chains overlap."""
+        st = self.step
+        main = torch.cuda.current_stream()
+        side = torch.cuda.Stream()
+        # every graph variant exists before the two streams start
+        for s in range(len(self.calls)):
+            dt, start = self.calls[s]
+            if (dt, start) not in self._ag:
+                self._adj_call(cur, next_ps, a_ga, a_gb, s)
+        side.wait_stream(main)
+        # stored states made on the main stream are read (and dropped) by the
+        # side stream: their memory must not be reused before it is done
+        for pair in list(slots.values()) + [cur]:
+            for x in _flat(*pair):
+                x.record_stream(side)
+        ring = [(self._own(cur[0]), self._own(cur[1])) for _ in range(depth)]
+        freed = [None] * depth
+        acc, k = None, 0
+        for act in self.actions[i:]:
+            if act[0] != "adjoint":
+                with torch.cuda.stream(side):
+                    cur, pos = self._do(act, cur, pos, slots, h)
+                continue
+            s = act[1]
+            if pos != s:
+                raise RuntimeError(f"checkpoint schedule out of step: at {pos}, reversing {s}")
+            slot = k % depth
+            with torch.cuda.stream(side):
+                if freed[slot] is not None:
+                    side.wait_event(freed[slot])
+                torch._foreach_copy_(_flat(*ring[slot]), _flat(*cur))
+                ready = torch.cuda.Event()
+                ready.record(side)
+            main.wait_event(ready)
+            a_ga, a_gb, a_wt = self._adj_call(ring[slot], next_ps, a_ga, a_gb, s)
+            acc = a_wt.clone() if acc is None else acc + a_wt
+            next_ps = ring[slot][0].ps.clone()
+            freed[slot] = torch.cuda.Event()
+            freed[slot].record(main)
+            pos, k = None, k + 1
+        main.wait_stream(side)
         return st.tr.grid_to_wave_T(acc)
 
     def value_and_grad(self, heating):
@@ -475,7 +632,7 @@ class ForcingGradient:
         z = st.zero_state()
         cur, dcur = (z, z), (z, z)
         for dt, start in self.calls:
-            nxt = st.forward(*cur, dt, start, h)
+            nxt = st.forward(*cur, dt, start, h)      # eager: the trajectory is kept
             dcur = st.tangent(cur[0], cur[1], nxt[0].ps, *dcur, dt, start, dfrc=d)
             cur = nxt
         return self.response(dcur[0])
@@ -485,8 +642,8 @@ class ForcingGradient:
         h = self._heating(heating)
         z = self.step.zero_state()
         cur = (z, z)
-        for dt, start in self.calls:
-            cur = self.step.forward(*cur, dt, start, h)
+        for s in range(len(self.calls)):
+            cur = self._fwd_call(cur, s, h)
         return self.response(cur[0])
 
 
