@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--adjoint", action="store_true",
                     help="checkpointed-adjoint cost and accuracy (T42L20, 20 days, FP64, "
                          "32 stored states) instead of the bench")
+    ap.add_argument("--adjoint-steps", type=int, default=None,
+                    help="--adjoint over this many steps instead of 20 days (profiling)")
     ap.add_argument("--fd-dirs", type=int, default=4,
                     help="central-difference directions checked by --adjoint")
     ap.add_argument("--sweep", action="store_true",
@@ -313,7 +315,7 @@ def precision_sweep(torch):
     return out
 
 
-def adjoint_measurement(torch, days=20.0, snaps=32, fd_dirs=4):
+def adjoint_measurement(torch, days=20.0, snaps=32, fd_dirs=4, nsteps=None):
     """Gradient of the area-mean day-20 streamfunction at sigma 0.25 over
     30-60N 150-210E with respect to the 20 x 64 x 128 heating (solid-body
     basic state, elliptic heating, plain damping, T42L20, FP64), by the
@@ -335,6 +337,8 @@ def adjoint_measurement(torch, days=20.0, snaps=32, fd_dirs=4):
     resp = AreaMeanStreamfunction(sp, vg)
     warm = ForcingGradient(model, resp, nsteps=4, snaps=2)
     warm.value_and_grad(heat)                        # captures every graph variant
+    if nsteps is not None:
+        days = nsteps / model.cfg.steps_per_day
     fg = ForcingGradient(model, resp, ndays=days, snaps=snaps)
     fg._fg, fg._ag = warm._fg, warm._ag
 
@@ -390,7 +394,7 @@ def main():
     if args.adjoint:
         import torch
         torch.cuda.set_device(0)
-        out = adjoint_measurement(torch, fd_dirs=args.fd_dirs)
+        out = adjoint_measurement(torch, fd_dirs=args.fd_dirs, nsteps=args.adjoint_steps)
         print(json.dumps({"adjoint": out}), flush=True)
         return
     if args.sweep:

@@ -59,6 +59,13 @@ def _ns(**kw):
     return types.SimpleNamespace(**kw)
 
 
+def _cat(xs):
+    """Concatenate fields along their last (level) axis; 2-D fields count as
+    one level.  Transforms act column by column, so one launch over the
+    concatenation gives each field exactly what its own launch would."""
+    return torch.cat([x if x.dim() == 3 else x.unsqueeze(-1) for x in xs], dim=-1)
+
+
 def state_dot(a, b):
     """Euclidean inner product of two grid states (u v t q ps)."""
     return sum(float((getattr(a, k) * getattr(b, k)).sum()) for k in FIELDS)
@@ -209,13 +216,30 @@ class TimeStep:
 
     # ---- forward ------------------------------------------------------------
     def forward(self, ga, gb, dt, start, frc_t):
-        """(ga, gb) -> (ga', gb') for one call of the reference loop."""
-        m, sp = self.m, self.sp
-        tend = m.dyn.tendencies(ga, frc_t=frc_t)
-        new = m.integ.step(dt, gb.to_spectral(sp), tend)
+        """(ga, gb) -> (ga', gb') for one call of the reference loop: the
+        operations of Dynamics.tendencies(ga), gb.to_spectral(),
+        Integrator.step and load_spectral, with the transforms of one kind
+        that share a call made in one launch over concatenated columns."""
+        m, sp, K = self.m, self.sp, self.vg.kmax
+        vo, di = sp.uv_to_vordiv(_cat([ga.u, gb.u]), _cat([ga.v, gb.v]))
+        s = sp.grid_to_wave(_cat([ga.lnps_pert(), gb.t, gb.q, gb.lnps_pert()]))
+        g = sp.wave_to_grid(_cat([vo[..., :K], di[..., :K]]))
+        pix, piy = sp.hgrad(s[..., 0])
+        o = m.dyn._grid_kernel(ga, g[..., :K], g[..., K:], pix, piy, frc_t, None, None,
+                               want_omega=False)
+        w = sp.grid_to_wave(_cat([o["gt_pi"], o["gt"], o["ke"], o["g"]]))
+        fvo, fdi = sp.uv_to_vordiv(_cat([o["fu"], o["xu"], o["yu"]]),
+                                   _cat([o["fv"], o["xv"], o["yv"]]))
+        tend = (fvo[..., :K], fdi[..., :K] - sp.laplacian(w[..., K + 1:2 * K + 1]),
+                -fdi[..., K:2 * K] + w[..., 1:K + 1], w[..., 0],
+                -fdi[..., 2 * K:] + w[..., 2 * K + 1:])
+        prev = {"vor": vo[..., K:], "div": di[..., K:], "t": s[..., 1:K + 1],
+                "pi": s[..., 2 * K + 1], "q": s[..., K + 1:2 * K + 1]}
+        new = m.integ.step(dt, prev, tend)
         u, v = sp.vordiv_to_uv(new["vor"], new["div"])
-        gc = self._state(u, v, sp.wave_to_grid(new["t"]), sp.wave_to_grid(new["q"]),
-                         self.ps_bar * (torch.exp(sp.wave_to_grid(new["pi"])) - 1.0))
+        gg = sp.wave_to_grid(_cat([new["t"], new["q"], new["pi"]]))
+        gc = self._state(u, v, gg[..., :K], gg[..., K:2 * K],
+                         self.ps_bar * (torch.exp(gg[..., 2 * K]) - 1.0))
         gb_new = ga if start else self._ra(gb, ga, gc)
         return gc, gb_new
 
@@ -347,20 +371,33 @@ class TimeStep:
             a_c = _ns(**{k: getattr(a_ga, k) + g * getattr(a_gb, k) for k in FIELDS})
             a_a = _ns(**{k: (1.0 - 2.0 * g) * getattr(a_gb, k) for k in FIELDS})
             a_b = _ns(**{k: g * getattr(a_gb, k) for k in FIELDS})
+        K, sp = self.vg.kmax, self.sp
         # load_spectral
         an_vor, an_div = tr.vordiv_to_uv_T(a_c.u, a_c.v)
-        an = {"vor": an_vor, "div": an_div, "t": tr.wave_to_grid_T(a_c.t),
-              "q": tr.wave_to_grid_T(a_c.q),
-              "pi": tr.wave_to_grid_T(a_c.ps * (self.ps_bar + gc_ps))}
+        x = tr.wave_to_grid_T(_cat([a_c.t, a_c.q, a_c.ps * (self.ps_bar + gc_ps)]))
+        an = {"vor": an_vor, "div": an_div, "t": x[..., :K], "q": x[..., K:2 * K],
+              "pi": x[..., 2 * K]}
         ap, aw = self._implicit_adjoint(dt, an)
-        # to_spectral of gb
-        bu, bv = tr.uv_to_vordiv_T(ap["vor"], ap["div"])
-        b = _ns(u=bu, v=bv, t=tr.grid_to_wave_T(ap["t"]), q=tr.grid_to_wave_T(ap["q"]),
-                ps=tr.grid_to_wave_T(ap["pi"]) / (self.ps_bar + gb.ps))
+        # grid-to-wave transposes of the tendencies of ga and of gb.to_spectral
+        y = tr.grid_to_wave_T(_cat([aw["pi"], aw["t"], -sp.laplacian(aw["div"]), aw["q"],
+                                    ap["t"], ap["q"], ap["pi"]]))
+        z = torch.zeros_like(aw["t"])
+        fu, fv = tr.uv_to_vordiv_T(_cat([aw["vor"], z, z]),
+                                   _cat([aw["div"], -aw["t"], -aw["q"]]))
+        a_o = {"gt_pi": y[..., 0], "gt": y[..., 1:K + 1], "ke": y[..., K + 1:2 * K + 1],
+               "g": y[..., 2 * K + 1:3 * K + 1], "fu": fu[..., :K], "fv": fv[..., :K],
+               "xu": fu[..., K:2 * K], "xv": fv[..., K:2 * K], "yu": fu[..., 2 * K:],
+               "yv": fv[..., 2 * K:]}
+        g = self._tend_adjoint_kernel(ga, a_o)
+        a_ps = tr.grid_to_wave_T(tr.hgrad_T(g["pix"], g["piy"])) / (self.ps_bar + ga.ps)
+        w2 = tr.wave_to_grid_T(_cat([g["vor"], g["div"]]))
+        uu, vv = tr.uv_to_vordiv_T(_cat([ap["vor"], w2[..., :K]]),
+                                   _cat([ap["div"], w2[..., K:]]))
+        b = _ns(u=uu[..., :K], v=vv[..., :K], t=y[..., 3 * K + 1:4 * K + 1],
+                q=y[..., 4 * K + 1:5 * K + 1], ps=y[..., 5 * K + 1] / (self.ps_bar + gb.ps))
         if a_b is not None:
             b = _ns(**{k: getattr(b, k) + getattr(a_b, k) for k in FIELDS})
-        # tendencies of ga
-        ta = self.adjoint_tendencies(ga, (aw["vor"], aw["div"], aw["t"], aw["pi"], aw["q"]))
+        ta = _ns(u=g["u"] + uu[..., K:], v=g["v"] + vv[..., K:], t=g["t"], q=g["q"], ps=a_ps)
         a_prev = _ns(**{k: getattr(ta, k) + getattr(a_a, k) for k in FIELDS})
         return a_prev, b, aw["t"]
 
@@ -586,13 +623,16 @@ class ForcingGradient:
             dt, start = self.calls[s]
             if (dt, start) not in self._ag:
                 self._adj_call(cur, next_ps, a_ga, a_gb, s)
+        # the ring is made on the main stream before the side stream is
+        # ordered after it: the side stream's first copies into the ring must
+        # not overtake these clones
+        ring = [(self._own(cur[0]), self._own(cur[1])) for _ in range(depth)]
         side.wait_stream(main)
         # stored states made on the main stream are read (and dropped) by the
         # side stream: their memory must not be reused before it is done
         for pair in list(slots.values()) + [cur]:
             for x in _flat(*pair):
                 x.record_stream(side)
-        ring = [(self._own(cur[0]), self._own(cur[1])) for _ in range(depth)]
         freed = [None] * depth
         acc, k = None, 0
         for act in self.actions[i:]:

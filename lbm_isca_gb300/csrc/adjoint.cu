@@ -9,7 +9,9 @@
 
 namespace lbm {
 
-constexpr int ADJ_THREADS = 128;
+// 32-thread blocks: one member's columns (8192 at T42) or coefficients
+// (3698) spread over all SMs instead of filling a few.
+constexpr int ADJ_THREADS = 32;
 
 // One thread per grid column (member, latitude, longitude).
 template <typename R, int KM>

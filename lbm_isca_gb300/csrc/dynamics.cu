@@ -204,7 +204,7 @@ int lbm_tendency_grid(int prec, const lbm_tend_grid_args* a, void* stream) {
     return LBM_ERR_ARG;
   if ((a->lin_u == nullptr) != (a->lin_v == nullptr)) return LBM_ERR_ARG;
   const size_t cols = (size_t)a->nmem * a->nlat * a->nlon;
-  const int threads = 128;
+  const int threads = 32;   // one member's 8192 columns (T42) over all SMs
   const unsigned blocks = (unsigned)((cols + threads - 1) / threads);
   if (prec == LBM_F64)
     k_tendency_grid<double><<<blocks, threads, 0, (cudaStream_t)stream>>>(*a);

@@ -279,6 +279,25 @@ def test_tendency_and_implicit_adjoints_dot_products(torch_cuda):
 
 
 @pytest.mark.gpu
+def test_step_forward_matches_the_general_loop(torch_cuda):
+    """TimeStep.forward (transforms of one kind batched per call) against
+    the model's own reference-sequence step, start-up and leapfrog calls."""
+    from lbm_isca_gb300 import configs
+    from lbm_isca_gb300.adjoint import FIELDS, TimeStep
+    m, sigm = _model()
+    st, r = TimeStep(m), _Rand(torch_cuda, 4)
+    heat = torch_cuda.as_tensor(configs.elliptic_heating(64, 32, sigm)).cuda()
+    ga, gb = r.state(st, 5.0), r.state(st, 5.0)
+    for start, dt in ((True, 300.0), (False, 1200.0)):
+        gc, gbn = st.forward(ga, gb, dt, start, heat)
+        m.ga, m.gb = ga.copy(), gb.copy()
+        m._general_step(dt, start, heat, None)
+        for k in FIELDS:
+            for got, ref in ((getattr(gc, k), getattr(m.ga, k)), (getattr(gbn, k), getattr(m.gb, k))):
+                assert float((got - ref).abs().max()) <= 1e-13 * float(ref.abs().max()), k
+
+
+@pytest.mark.gpu
 def test_step_adjoint_dot_product_and_taylor(torch_cuda):
     """Whole step: <TL dx, y> = <dx, ADJ y> to 1e-10 (start-up and leapfrog
     calls), and the TL is the derivative of the nonlinear step."""
