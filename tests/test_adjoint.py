@@ -407,6 +407,14 @@ def test_checkpointing_changes_nothing(gradient_case, torch_cuda):
     assert abs(float(J2) - c.J) <= 1e-13 * abs(c.J)
     assert float((g2 - c.grad).abs().max()) <= 1e-13 * float(c.grad.abs().max())
     assert full.forward_steps == len(full.calls)       # every state stored: no re-steps
+    # every state stored, two streams against one: the reverse sweep's
+    # hand-over ring must not race with its own initialisation
+    for pipe in (True, False):
+        g = ForcingGradient(c.m, c.resp, nsteps=6, snaps=32, pipeline=pipe).value_and_grad(
+            c.heat)[1]
+        if pipe:
+            g_pipe = g
+    assert bool((g_pipe == g).all())
     h = c.heat.clone().requires_grad_(True)
     HeatingResponse.apply(h, ForcingGradient(c.m, c.resp, nsteps=36, snaps=3)).backward()
     assert float((h.grad - c.grad).abs().max()) <= 1e-13 * float(c.grad.abs().max())
