@@ -55,6 +55,9 @@ def parse():
                          "32 stored states) instead of the bench")
     ap.add_argument("--adjoint-steps", type=int, default=None,
                     help="--adjoint over this many steps instead of 20 days (profiling)")
+    ap.add_argument("--adjoint-members", type=int, default=None,
+                    help="--adjoint: time one gradient of this many members (own heatings) "
+                         "against one single-member gradient instead")
     ap.add_argument("--fd-dirs", type=int, default=4,
                     help="central-difference directions checked by --adjoint")
     ap.add_argument("--sweep", action="store_true",
@@ -389,8 +392,57 @@ def adjoint_measurement(torch, days=20.0, snaps=32, fd_dirs=4, nsteps=None):
     }
 
 
+def adjoint_batched_measurement(torch, nmem, nsteps, snaps=32):
+    """One gradient of ``nmem`` members (seeded ensemble heatings, T42L20,
+    FP64, each member its own response) reversed together, against one
+    single-member gradient over the same calls."""
+    from lbm_isca_gb300 import LBM, Config, Spectral, VerticalGrid, configs
+    from lbm_isca_gb300.adjoint import AreaMeanStreamfunction, ForcingGradient
+    from lbm_isca_gb300.ensemble import make_ensemble_model
+    K = K_LEV
+    sigm = configs.equal_sigma_half_levels(K)
+    bs = configs.solid_body_basic_state(128, 64, sigm)
+    heats = torch.as_tensor(configs.ensemble_heating(128, 64, sigm, nmem, seed=SEED)[0],
+                            device="cuda")
+    cfg = lambda: Config(**configs.plain_damping(K))   # noqa: E731
+    out = {"members": nmem, "calls": nsteps + 2, "snaps": snaps}
+    runs = (("single", None), ("batched", nmem))
+    for name, E in runs:
+        if E is None:
+            sp, vg = Spectral(), VerticalGrid(sigm=sigm)
+            m = LBM(bs, sp, vg, cfg())
+            h = heats[0]
+        else:
+            m, sp, vg = make_ensemble_model(bs, E, cfg(), device="cuda", sigm=sigm)
+            h = heats
+        resp = AreaMeanStreamfunction(sp, vg)
+        warm = ForcingGradient(m, resp, nsteps=4, snaps=2)
+        warm.value_and_grad(h)
+        fg = ForcingGradient(m, resp, nsteps=nsteps, snaps=snaps)
+        fg._fg, fg._ag = warm._fg, warm._ag
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        J, g = fg.value_and_grad(h)
+        torch.cuda.synchronize()
+        out[f"{name}_gradient_s"] = time.perf_counter() - t0
+        out[f"{name}_J0"] = float(J.reshape(-1)[0])
+        out[f"{name}_grad0_absmax"] = float(g.reshape((-1,) + tuple(g.shape[-3:]))[0].abs().max())
+    out["member_gradients_per_s_single"] = 1.0 / out["single_gradient_s"]
+    out["member_gradients_per_s_batched"] = nmem / out["batched_gradient_s"]
+    out["speedup_per_member"] = (out["member_gradients_per_s_batched"]
+                                 / out["member_gradients_per_s_single"])
+    return out
+
+
 def main():
     args = parse()
+    if args.adjoint and args.adjoint_members:
+        import torch
+        torch.cuda.set_device(0)
+        out = adjoint_batched_measurement(torch, args.adjoint_members,
+                                          args.adjoint_steps or 72)
+        print(json.dumps({"adjoint_batched": out}), flush=True)
+        return
     if args.adjoint:
         import torch
         torch.cuda.set_device(0)

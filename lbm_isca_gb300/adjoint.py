@@ -59,11 +59,12 @@ def _ns(**kw):
     return types.SimpleNamespace(**kw)
 
 
-def _cat(xs):
-    """Concatenate fields along their last (level) axis; 2-D fields count as
-    one level.  Transforms act column by column, so one launch over the
-    concatenation gives each field exactly what its own launch would."""
-    return torch.cat([x if x.dim() == 3 else x.unsqueeze(-1) for x in xs], dim=-1)
+def _cat(xs, nd=3):
+    """Concatenate fields along their last (level) axis; a field of fewer
+    than ``nd`` dimensions (a surface field) counts as one level.  Transforms
+    act column by column, so one launch over the concatenation gives each
+    field exactly what its own launch would."""
+    return torch.cat([x if x.dim() == nd else x.unsqueeze(-1) for x in xs], dim=-1)
 
 
 def state_dot(a, b):
@@ -156,12 +157,15 @@ class AdjointTransforms:
 # The time step, its tangent-linear model and its adjoint
 # ---------------------------------------------------------------------------
 class TimeStep:
-    """One reference step on grid states of an ``LBM`` (FP64, one member)."""
+    """One reference step on grid states of an ``LBM`` (FP64): one member,
+    or E members (a batched model, ``make_ensemble_model``) whose states
+    carry a leading member axis and advance together; members share the
+    basic state and operators and are otherwise independent."""
 
     def __init__(self, model):
-        if model.batched:
-            raise ValueError("the adjoint takes a single-member model")
         self.m = model
+        self.nmem = model.nmem if model.batched else 1
+        self.nd = 4 if model.batched else 3     # dimensions of a level-carrying field
         self.sp, self.vg = model.sp, model.vg
         self.tr = AdjointTransforms(model.sp)
         self.ps_bar = model.ga.ps_bar
@@ -202,12 +206,14 @@ class TimeStep:
         st.u, st.v, st.t, st.q, st.ps = u, v, t, q, ps
         return st
 
+    def _lead(self):
+        return (self.nmem,) if self.nd == 4 else ()
+
     def zero_state(self):
         J, I, K = self.sp.nlat, self.sp.nlon, self.vg.kmax
-        z3 = lambda: torch.zeros((J, I, K), dtype=torch.float64,   # noqa: E731
-                                 device=self.sp.device)
-        return self._state(z3(), z3(), z3(), z3(),
-                           torch.zeros((J, I), dtype=torch.float64, device=self.sp.device))
+        f64 = dict(dtype=torch.float64, device=self.sp.device)
+        z3 = lambda: torch.zeros(self._lead() + (J, I, K), **f64)   # noqa: E731
+        return self._state(z3(), z3(), z3(), z3(), torch.zeros(self._lead() + (J, I), **f64))
 
     def _ra(self, prev, cur, nxt):
         g = self.gamma
@@ -220,16 +226,16 @@ class TimeStep:
         operations of Dynamics.tendencies(ga), gb.to_spectral(),
         Integrator.step and load_spectral, with the transforms of one kind
         that share a call made in one launch over concatenated columns."""
-        m, sp, K = self.m, self.sp, self.vg.kmax
-        vo, di = sp.uv_to_vordiv(_cat([ga.u, gb.u]), _cat([ga.v, gb.v]))
-        s = sp.grid_to_wave(_cat([ga.lnps_pert(), gb.t, gb.q, gb.lnps_pert()]))
-        g = sp.wave_to_grid(_cat([vo[..., :K], di[..., :K]]))
+        m, sp, K, nd = self.m, self.sp, self.vg.kmax, self.nd
+        vo, di = sp.uv_to_vordiv(_cat([ga.u, gb.u], nd), _cat([ga.v, gb.v], nd))
+        s = sp.grid_to_wave(_cat([ga.lnps_pert(), gb.t, gb.q, gb.lnps_pert()], nd))
+        g = sp.wave_to_grid(_cat([vo[..., :K], di[..., :K]], nd))
         pix, piy = sp.hgrad(s[..., 0])
         o = m.dyn._grid_kernel(ga, g[..., :K], g[..., K:], pix, piy, frc_t, None, None,
                                want_omega=False)
-        w = sp.grid_to_wave(_cat([o["gt_pi"], o["gt"], o["ke"], o["g"]]))
-        fvo, fdi = sp.uv_to_vordiv(_cat([o["fu"], o["xu"], o["yu"]]),
-                                   _cat([o["fv"], o["xv"], o["yv"]]))
+        w = sp.grid_to_wave(_cat([o["gt_pi"], o["gt"], o["ke"], o["g"]], nd))
+        fvo, fdi = sp.uv_to_vordiv(_cat([o["fu"], o["xu"], o["yu"]], nd),
+                                   _cat([o["fv"], o["xv"], o["yv"]], nd))
         tend = (fvo[..., :K], fdi[..., :K] - sp.laplacian(w[..., K + 1:2 * K + 1]),
                 -fdi[..., K:2 * K] + w[..., 1:K + 1], w[..., 0],
                 -fdi[..., 2 * K:] + w[..., 2 * K + 1:])
@@ -237,7 +243,7 @@ class TimeStep:
                 "pi": s[..., 2 * K + 1], "q": s[..., K + 1:2 * K + 1]}
         new = m.integ.step(dt, prev, tend)
         u, v = sp.vordiv_to_uv(new["vor"], new["div"])
-        gg = sp.wave_to_grid(_cat([new["t"], new["q"], new["pi"]]))
+        gg = sp.wave_to_grid(_cat([new["t"], new["q"], new["pi"]], nd))
         gc = self._state(u, v, gg[..., :K], gg[..., K:2 * K],
                          self.ps_bar * (torch.exp(gg[..., 2 * K]) - 1.0))
         gb_new = ga if start else self._ra(gb, ga, gc)
@@ -286,9 +292,10 @@ class TimeStep:
         sp, vg, bs = self.sp, self.vg, self.m.bst
         J, I, K = sp.nlat, sp.nlon, vg.kmax
         f64 = dict(device=sp.device, dtype=torch.float64)
-        out = {k: torch.empty((J, I, K), **f64) for k in ("u", "v", "t", "q", "vor", "div")}
-        out["pix"] = torch.empty((J, I), **f64)
-        out["piy"] = torch.empty((J, I), **f64)
+        lead = self._lead()
+        out = {k: torch.empty(lead + (J, I, K), **f64) for k in ("u", "v", "t", "q", "vor", "div")}
+        out["pix"] = torch.empty(lead + (J, I), **f64)
+        out["piy"] = torch.empty(lead + (J, I), **f64)
         keep = []
 
         def c(x):
@@ -297,7 +304,7 @@ class TimeStep:
             return ptr(t)
 
         a = TendAdjArgs()
-        a.nmem, a.nlat, a.nlon, a.kmax = 1, J, I, K
+        a.nmem, a.nlat, a.nlon, a.kmax = self.nmem, J, I, K
         a.kappa, a.epsvt, a.rair = KAPPA, EPSVT, RAIR
         a.dsig, a.sigm, a.alpha, a.w3, a.wP = (c(vg.dsig), c(vg.sigm), c(vg.alpha), c(vg.w3),
                                                c(vg.wP))
@@ -344,7 +351,7 @@ class TimeStep:
         keep = [vg.ww.contiguous(), vg.tmtx.contiguous(), vg.gg.contiguous(),
                 vg.dsig.contiguous()]
         a = ImplicitAdjArgs()
-        a.nmem, a.nmax, a.kmax, a.dt = 1, sp.nmax, vg.kmax, float(dt)
+        a.nmem, a.nmax, a.kmax, a.dt = self.nmem, sp.nmax, vg.kmax, float(dt)
         a.lap, a.kv, a.kd, a.ktt, a.kq = (ptr(sp.laplace), ptr(dmp.kv), ptr(dmp.kd),
                                           ptr(dmp.ktt), ptr(dmp.kq))
         a.ww, a.tmtx, a.gg, a.dsig = (ptr(x) for x in keep)
@@ -371,28 +378,28 @@ class TimeStep:
             a_c = _ns(**{k: getattr(a_ga, k) + g * getattr(a_gb, k) for k in FIELDS})
             a_a = _ns(**{k: (1.0 - 2.0 * g) * getattr(a_gb, k) for k in FIELDS})
             a_b = _ns(**{k: g * getattr(a_gb, k) for k in FIELDS})
-        K, sp = self.vg.kmax, self.sp
+        K, sp, nd = self.vg.kmax, self.sp, self.nd
         # load_spectral
         an_vor, an_div = tr.vordiv_to_uv_T(a_c.u, a_c.v)
-        x = tr.wave_to_grid_T(_cat([a_c.t, a_c.q, a_c.ps * (self.ps_bar + gc_ps)]))
+        x = tr.wave_to_grid_T(_cat([a_c.t, a_c.q, a_c.ps * (self.ps_bar + gc_ps)], nd))
         an = {"vor": an_vor, "div": an_div, "t": x[..., :K], "q": x[..., K:2 * K],
               "pi": x[..., 2 * K]}
         ap, aw = self._implicit_adjoint(dt, an)
         # grid-to-wave transposes of the tendencies of ga and of gb.to_spectral
         y = tr.grid_to_wave_T(_cat([aw["pi"], aw["t"], -sp.laplacian(aw["div"]), aw["q"],
-                                    ap["t"], ap["q"], ap["pi"]]))
+                                    ap["t"], ap["q"], ap["pi"]], nd))
         z = torch.zeros_like(aw["t"])
-        fu, fv = tr.uv_to_vordiv_T(_cat([aw["vor"], z, z]),
-                                   _cat([aw["div"], -aw["t"], -aw["q"]]))
+        fu, fv = tr.uv_to_vordiv_T(_cat([aw["vor"], z, z], nd),
+                                   _cat([aw["div"], -aw["t"], -aw["q"]], nd))
         a_o = {"gt_pi": y[..., 0], "gt": y[..., 1:K + 1], "ke": y[..., K + 1:2 * K + 1],
                "g": y[..., 2 * K + 1:3 * K + 1], "fu": fu[..., :K], "fv": fv[..., :K],
                "xu": fu[..., K:2 * K], "xv": fv[..., K:2 * K], "yu": fu[..., 2 * K:],
                "yv": fv[..., 2 * K:]}
         g = self._tend_adjoint_kernel(ga, a_o)
         a_ps = tr.grid_to_wave_T(tr.hgrad_T(g["pix"], g["piy"])) / (self.ps_bar + ga.ps)
-        w2 = tr.wave_to_grid_T(_cat([g["vor"], g["div"]]))
-        uu, vv = tr.uv_to_vordiv_T(_cat([ap["vor"], w2[..., :K]]),
-                                   _cat([ap["div"], w2[..., K:]]))
+        w2 = tr.wave_to_grid_T(_cat([g["vor"], g["div"]], nd))
+        uu, vv = tr.uv_to_vordiv_T(_cat([ap["vor"], w2[..., :K]], nd),
+                                   _cat([ap["div"], w2[..., K:]], nd))
         b = _ns(u=uu[..., :K], v=vv[..., :K], t=y[..., 3 * K + 1:4 * K + 1],
                 q=y[..., 4 * K + 1:5 * K + 1], ps=y[..., 5 * K + 1] / (self.ps_bar + gb.ps))
         if a_b is not None:
@@ -428,12 +435,13 @@ class AreaMeanStreamfunction:
         sp = self.sp
         vor, _ = sp.uv_to_vordiv(st.u, st.v)
         psi = sp.wave_to_grid(sp.inverse_laplacian(vor))
-        return (psi * self.weights).sum()
+        return (psi * self.weights).sum(dim=(-3, -2, -1))     # one value per member
 
     def seed(self, tr, like):
         """Adjoint grid state of the response (d J / d final state)."""
         sp = self.sp
-        a_vor = sp.inverse_laplacian(tr.wave_to_grid_T(self.weights))
+        a_vor = sp.inverse_laplacian(tr.wave_to_grid_T(self.weights.expand_as(like.u)
+                                                       .contiguous()))
         u, v = tr.uv_to_vordiv_T(a_vor, torch.zeros_like(a_vor))
         a = _zeros_like_state(like)
         a.u, a.v = u, v
@@ -496,9 +504,10 @@ class ForcingGradient:
     def _heating(self, heating):
         sp, vg = self.step.sp, self.step.vg
         h = to_device(heating, sp.device)
-        if tuple(h.shape) != (sp.nlat, sp.nlon, vg.kmax):
-            raise ValueError(f"heating must be (nlat, nlon, kmax) = "
-                             f"{(sp.nlat, sp.nlon, vg.kmax)}, got {tuple(h.shape)}")
+        want = self.step._lead() + (sp.nlat, sp.nlon, vg.kmax)
+        if tuple(h.shape) != want:
+            raise ValueError(f"heating must be ([nmem,] nlat, nlon, kmax) = {want}, "
+                             f"got {tuple(h.shape)}")
         return h.contiguous()
 
     def _fwd_call(self, cur, s, h):
@@ -688,16 +697,18 @@ class ForcingGradient:
 
 
 class HeatingResponse(torch.autograd.Function):
-    """``J = HeatingResponse.apply(heating, grad_driver)``; ``J.backward()``
+    """``J = HeatingResponse.apply(heating, gradient)`` with a
+    ``ForcingGradient``; ``J.backward()``
     runs the checkpointed adjoint and fills ``heating.grad``."""
 
     @staticmethod
-    def forward(ctx, heating, driver):
-        ctx.driver = driver
+    def forward(ctx, heating, gradient):
+        ctx.gradient = gradient
         with torch.no_grad():
-            return driver.forward(heating.detach())
+            return gradient.forward(heating.detach())
 
     @staticmethod
     def backward(ctx, gJ):
-        g = ctx.driver.backward()
+        g = ctx.gradient.backward()
+        gJ = gJ.reshape(gJ.shape + (1,) * (g.dim() - gJ.dim()))   # one J per member
         return gJ * g, None

@@ -418,3 +418,35 @@ def test_checkpointing_changes_nothing(gradient_case, torch_cuda):
     h = c.heat.clone().requires_grad_(True)
     HeatingResponse.apply(h, ForcingGradient(c.m, c.resp, nsteps=36, snaps=3)).backward()
     assert float((h.grad - c.grad).abs().max()) <= 1e-13 * float(c.grad.abs().max())
+
+
+@pytest.mark.gpu
+def test_batched_gradient_matches_single_members(torch_cuda):
+    """E members with their own heatings reversed together: each member's J
+    and gradient equal its own single-member run; the tangent-linear
+    response of each member equals its gradient's dot product."""
+    from lbm_isca_gb300 import LBM, Config, Spectral, VerticalGrid, configs
+    from lbm_isca_gb300.adjoint import AreaMeanStreamfunction, ForcingGradient
+    from lbm_isca_gb300.ensemble import make_ensemble_model
+    torch = torch_cuda
+    K, E = 20, 3
+    sigm = configs.equal_sigma_half_levels(K)
+    bs = configs.solid_body_basic_state(64, 32, sigm)
+    heats = torch.as_tensor(configs.ensemble_heating(64, 32, sigm, E, seed=4)[0]).cuda()
+    mk = lambda: Config(ndays=1.0, **configs.plain_damping(K))   # noqa: E731
+    mb, spb, vgb = make_ensemble_model(bs, E, mk(), device="cuda", nlon=64, nlat=32, nmax=21,
+                                       sigm=sigm)
+    fb = ForcingGradient(mb, AreaMeanStreamfunction(spb, vgb), nsteps=24, snaps=5)
+    Jb, gb = fb.value_and_grad(heats)
+    assert tuple(Jb.shape) == (E,) and tuple(gb.shape) == tuple(heats.shape)
+    sp, vg = Spectral(nlon=64, nlat=32, nmax=21), VerticalGrid(sigm=sigm)
+    m1 = LBM(bs, sp, vg, mk())
+    for e in range(E):
+        J1, g1 = ForcingGradient(m1, AreaMeanStreamfunction(sp, vg), nsteps=24,
+                                 snaps=5).value_and_grad(heats[e])
+        assert abs(float(J1) - float(Jb[e])) <= 1e-12 * abs(float(J1))
+        assert float((g1 - gb[e]).abs().max()) <= 1e-12 * float(g1.abs().max())
+    d = torch.as_tensor(np.random.default_rng(2).normal(size=tuple(heats.shape))).cuda()
+    tl = fb.tangent(heats, d * float(heats.abs().max()))
+    dots = (gb * d * float(heats.abs().max())).sum(dim=(1, 2, 3))
+    assert float(((tl - dots).abs() / dots.abs()).max()) < 1e-10
