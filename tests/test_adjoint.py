@@ -58,6 +58,120 @@ def test_binomial_schedule_meets_the_bound():
         simulate([("store", 0), ("advance", 1, 2)])
 
 
+class _ToyStep:
+    """A stand-in for TimeStep on CPU tensors with the same call structure:
+    a leapfrog-like nonlinear map of (ga, gb) forced by h, whose exact
+    adjoint is written out, so that the gradient driver's bookkeeping (which
+    stored state, which next-level ps each adjoint call gets) is checked
+    without the GPU."""
+
+    gamma = 0.1
+
+    def __init__(self, torch, shape):
+        self.torch, self.shape = torch, shape
+        # the heating enters the toy map directly: its transform is the identity
+        self.tr = types.SimpleNamespace(grid_to_wave_T=lambda x: x)
+
+    def _state(self, u, v, t, q, ps):
+        return types.SimpleNamespace(u=u, v=v, t=t, q=q, ps=ps)
+
+    def _lead(self):
+        return ()
+
+    def zero_state(self):
+        z = lambda: self.torch.zeros(self.shape, dtype=self.torch.float64)   # noqa: E731
+        return self._state(z(), z(), z(), z(), z())
+
+    @staticmethod
+    def _c(ga, gb, dt, h):
+        # next level: u' = u_b + dt (sin(u_a) + h), ps' = ps_b + dt u_a^2, the
+        # other fields carried along linearly
+        return (gb.u + dt * (ga.u.sin() + h), gb.v + dt * ga.u, gb.t + dt * ga.v,
+                gb.q + 0.5 * ga.t, gb.ps + dt * ga.u * ga.u)
+
+    def forward(self, ga, gb, dt, start, h):
+        gc = self._state(*self._c(ga, gb, dt, h))
+        if start:
+            return gc, ga
+        g = self.gamma
+        return gc, self._state(*(getattr(ga, k) + g * (getattr(gb, k) - 2 * getattr(ga, k)
+                                                       + getattr(gc, k)) for k in
+                                 ("u", "v", "t", "q", "ps")))
+
+    def adjoint(self, ga, gb, gc_ps, a_ga, a_gb, dt, start):
+        # the map is written as gc = C(ga, gb); gc_ps is checked against it
+        assert self.torch.equal(gc_ps, self._c(ga, gb, dt, 0.0)[4])
+        keys = ("u", "v", "t", "q", "ps")
+        g = self.gamma
+        if start:
+            ac, aa, ab = a_ga, a_gb, None
+        else:
+            ac = self._state(*(getattr(a_ga, k) + g * getattr(a_gb, k) for k in keys))
+            aa = self._state(*((1 - 2 * g) * getattr(a_gb, k) for k in keys))
+            ab = self._state(*(g * getattr(a_gb, k) for k in keys))
+        na = self._state(dt * ga.u.cos() * ac.u + dt * ac.v + 2 * dt * ga.u * ac.ps,
+                         dt * ac.t, 0.5 * ac.q, 0 * ac.q, 0 * ac.ps)
+        nb = self._state(ac.u, ac.v, ac.t, ac.q, ac.ps)
+        pa = self._state(*(getattr(na, k) + getattr(aa, k) for k in keys))
+        pb = nb if ab is None else self._state(*(getattr(nb, k) + getattr(ab, k) for k in keys))
+        return pa, pb, dt * ac.u
+
+
+def test_gradient_driver_bookkeeping_on_a_toy_model():
+    """The checkpointed gradient of a toy model equals central differences
+    and the every-state-stored gradient, for several stored-state counts."""
+    torch = pytest.importorskip("torch")
+    from lbm_isca_gb300.adjoint import ForcingGradient
+    from lbm_isca_gb300.checkpoint import schedule
+
+    shape = (3, 4)
+    calls = [(0.025, True), (0.05, True)] + [(0.1, False)] * 13
+
+    class Resp:
+        def __call__(self, st):
+            return (st.u * st.u).sum() + (st.ps * st.t).sum()
+
+        def seed(self, tr, like):
+            z = torch.zeros_like(like.u)
+            return types.SimpleNamespace(u=2 * like.u, v=z, t=like.ps, q=z, ps=like.t)
+
+    def driver(snaps):
+        fg = ForcingGradient.__new__(ForcingGradient)
+        fg.step, fg.response = _ToyStep(torch, shape), Resp()
+        fg.use_graph, fg.pipeline, fg._fg, fg._ag = False, False, {}, {}
+        fg.calls, fg.snaps = calls, snaps
+        fg.actions = schedule(len(calls), snaps)
+        fg.forward_steps, fg.peak_stored, fg._saved = 0, 0, None
+        fg._heating = lambda h: h
+        return fg
+
+    h = torch.as_tensor(np.random.default_rng(8).normal(size=shape))
+    ref = None
+    for snaps in (1, 2, 3, 5, 40):
+        fg = driver(snaps)
+        J, g = fg.value_and_grad(h)
+        assert fg.peak_stored <= snaps
+        if ref is None:
+            ref = g
+            d = torch.as_tensor(np.random.default_rng(9).normal(size=shape))
+            e = 1e-6
+            fd = (float(fg.value(h + e * d)) - float(fg.value(h - e * d))) / (2 * e)
+            assert abs(fd - float((g * d).sum())) <= 1e-7 * abs(fd)
+        else:
+            assert torch.allclose(g, ref, rtol=1e-13, atol=0)
+
+
+def test_response_box_sizes():
+    """30-60N x 150-210E: 6 x 11 points at T21, 11 x 21 at T42, 22 x 43 at T85."""
+    from lbm_isca_gb300.configs import response_box
+    from oracle.lbm_oracle import SphericalTransform
+    for (nlon, nlat, nmax), want in (((64, 32, 21), (6, 11)), ((128, 64, 42), (11, 21)),
+                                     ((256, 128, 85), (22, 43))):
+        tr = SphericalTransform(nlon, nlat, nmax)
+        box = response_box(np.degrees(tr.lat), np.degrees(tr.lon))
+        assert (int(box.any(axis=1).sum()), int(box.any(axis=0).sum())) == want
+
+
 @pytest.fixture(scope="module")
 def host_adjoint(tmp_path_factory):
     gxx = shutil.which("g++")
