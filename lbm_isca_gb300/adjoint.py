@@ -250,7 +250,9 @@ class TimeStep:
         return gc, gb_new
 
     # ---- tangent-linear -----------------------------------------------------
-    def _assemble(self, o, frc_vor=None, frc_div=None):
+    def _assemble(self, o):
+        """The spectral tendencies from the grid kernel's outputs, in the
+        operation order of Dynamics.tendencies (dynamics.py:186-262)."""
         sp = self.sp
         wt_pi = sp.grid_to_wave(o["gt_pi"])
         wt_t = sp.neg_divergence(o["xu"], o["xv"]) + sp.grid_to_wave(o["gt"])
