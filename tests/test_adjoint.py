@@ -11,7 +11,8 @@ tendency, implicit-update and whole-step adjoints against the tangent-linear
 model, the tangent-linear tendencies against the reference's own
 (``Dynamics(strictly_linear=True)``, golden fixture made by
 tests/golden/make_golden_adjoint.py) and the adjoint against it by a dot
-product, the whole-run tangent-linear response against the gradient, the
+product, the tangent-linear tendencies about a non-zero state against
+central differences of the reference's nonlinear tendency, the whole-run tangent-linear response against the gradient, the
 gradient against central finite differences along 16 seeded directions
 (eps = 1e-4 relative), and checkpointing that changes nothing.
 """
@@ -468,6 +469,36 @@ def test_adjoint_against_reference_tangent_linear(torch_cuda):
               for n, y in zip(names, ys))
     rhs = state_dot(dx, st.adjoint_tendencies(zero, ys))
     assert abs(lhs - rhs) <= 1e-10 * abs(lhs)
+
+
+@pytest.mark.gpu
+def test_tangent_linear_about_a_state_against_reference_tendency(torch_cuda):
+    """About a non-zero state (the reference's test direction at amplitude
+    0.5) the tangent-linear tendencies equal central differences of the
+    reference's own nonlinear tendency (kinetic energy kept, exact pi' <->
+    ps'), eps = 1e-4, along its second test direction."""
+    from lbm_isca_gb300 import LBM, Config, Spectral, VerticalGrid
+    from lbm_isca_gb300.adjoint import TimeStep
+    torch = torch_cuda
+    g = golden("adjoint_tl.npz")
+    J, I, K = 32, 64, 5
+    z3 = lambda p: np.broadcast_to(p[:, None, :], (J, I, K)).copy()   # noqa: E731
+    bs = types.SimpleNamespace(u=z3(g["bs_u"]), v=np.zeros((J, I, K)), t=z3(g["bs_t"]),
+                               q=z3(g["bs_q"]), ps=np.full((J, I), float(g["bs_ps"])))
+    sp, vg = Spectral(nlon=64, nlat=32, nmax=21), VerticalGrid(sigm=g["sigm"])
+    m = LBM(bs, sp, vg, Config(strictly_linear=False, sponge=False, ddragv=None,
+                               ddragd=None, ddragt=None))
+    st = TimeStep(m)
+    T = lambda a: torch.as_tensor(np.asarray(a)).cuda()   # noqa: E731
+    ps_bar = float(g["bs_ps"])
+    x0 = st._state(T(0.5 * g["u0"]), T(0.5 * g["v0"]), T(0.5 * g["t0"]), T(0.5 * g["q0"]),
+                   T(ps_bar * (np.exp(0.5 * g["pi0"]) - 1.0)))
+    # the reference perturbs pi'; in ps' that is (ps_bar + ps0) d_pi
+    dx = st._state(T(g["d_u"]), T(g["d_v"]), T(g["d_t"]), T(g["d_q"]),
+                   (st.ps_bar + x0.ps) * T(g["d_pi"]))
+    for n, x in zip(("vor", "div", "t", "pi", "q"), st.tangent_tendencies(x0, dx)):
+        ref = g["D_" + n]
+        assert np.abs(x.cpu().numpy() - ref).max() <= 1e-7 * np.abs(ref).max(), n
 
 
 @pytest.fixture(scope="module")
