@@ -37,6 +37,11 @@ UNIT = "member-steps/s"
 GRID = (128, 64, 42)
 K_LEV = 20
 SEED = 1
+DTYPES = {"fp32": "f32", "fp64": "f64", "bf16x3": "bf16x3 split, f32 accumulate",
+          "bf16split": "bf16x2 split, f32 accumulate"}
+LEGENDRE_NOTE = {"fp32": "on the FP32 FMA pipes", "fp64": "in FP64",
+                 "bf16x3": "on the tensor cores (tcgen05, bf16 3-way split, 6 products)",
+                 "bf16split": "on the tensor cores (tcgen05, bf16 2-way split, 3 products)"}
 
 
 def parse():
@@ -46,7 +51,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--members", type=int, default=512)
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--precision", default="fp32",
+                    choices=["fp32", "fp64", "bf16x3", "bf16split"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the accuracy / plain-FP64 / CPU side measurements")
@@ -60,6 +66,11 @@ def parse():
                          "against one single-member gradient instead")
     ap.add_argument("--fd-dirs", type=int, default=4,
                     help="central-difference directions checked by --adjoint")
+    ap.add_argument("--conditioning", action="store_true",
+                    help="conditioning of the 30-day problem: FP64 against FP64 with every "
+                         "heating rounded to FP32 (a relative input change below 2^-24), next "
+                         "to FP32 against FP64, T42L20 x 128 members (seed 2) and T85L40 x 8, "
+                         "reference dynamics and strictly linear, instead of the bench")
     ap.add_argument("--sweep", action="store_true",
                     help="precision sweep (FP32 vs FP64 per field at days 10 and 30, "
                          "T42L20 x 128 members and T85L40 x 16 members) instead of the bench")
@@ -248,20 +259,15 @@ def algorithmic_bytes(E, p):
 
 
 def read_traffic(kernel, E):
-    """dram bytes per launch from the committed ncu summary, scaled to E."""
-    path = os.path.join(ROOT, "profiles", "fp32_stepper_t42l20.md")
-    if not os.path.exists(path):
+    """DRAM bytes per launch of `kernel` from the committed ncu record
+    (profiles/dram_traffic_t42l20.json), scaled from its member count to E
+    (the traffic of every stepper kernel grows in proportion to the members)."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic_t42l20.json")
+    try:
+        rec = json.load(open(path))
+        return float(rec["bytes_per_launch"][kernel]) * E / float(rec["members"])
+    except Exception:
         return None
-    key = f"traffic[{kernel}]"
-    for line in open(path):
-        if line.strip().startswith(key):
-            try:
-                rhs = line.split("=", 1)[1].split()
-                val, members = float(rhs[0]), float(rhs[rhs.index("members") - 1])
-                return val * E / members
-            except Exception:
-                return None
-    return None
 
 
 def precision_sweep(torch):
@@ -315,6 +321,70 @@ def precision_sweep(torch):
                 rec[f"day{nday}"] = errs
             rec[f"run_s_day{nday}"] = secs
         out[name] = rec
+    return out
+
+
+def conditioning(torch, days=(10, 30)):
+    """How much of the FP32-against-FP64 difference the problem itself sets:
+    the same FP64 run with each heating rounded to FP32 (every input changed
+    by less than 2^-24 relatively, the size of one FP32 rounding) against
+    the unrounded FP64 run, beside the FP32 stepper against FP64; relative L2
+    per field over the packed spectral state of all members, at days 10 and
+    30.  Cases as the precision sweep: T42L20 x 128 members (dt 1200 s) with
+    the reference's dynamics (kinetic-energy term kept) and strictly linear,
+    T85L40 x 8 members (dt 600 s) strictly linear; seeded heatings (seed 2)."""
+    from lbm_isca_gb300 import configs
+    from lbm_isca_gb300.ensemble import make_ensemble_model
+    from lbm_isca_gb300.model import Config
+    out = {}
+    # (T85L40 with the reference dynamics grows without bound by day 14, in
+    # FP64 as in FP32: not a conditioning case)
+    cases = [(128, 64, 42, 20, 128, 1200.0, False), (128, 64, 42, 20, 128, 1200.0, True),
+             (256, 128, 85, 40, 8, 600.0, True)]
+    for (nlon, nlat, nmax, K, E, delt, lin) in cases:
+        sigm = configs.equal_sigma_half_levels(K)
+        bs = configs.solid_body_basic_state(nlon, nlat, sigm)
+        heats, _ = configs.ensemble_heating(nlon, nlat, sigm, E, seed=2)
+        spd = int(round(86400.0 / delt))
+        runs = {}
+        for name, prec, h in (("fp64", "fp64", heats),
+                              ("fp64_input_rounded", "fp64",
+                               heats.astype(np.float32).astype(np.float64)),
+                              ("fp32", "fp32", heats)):
+            cfg = Config(ndays=max(days), precision=prec,
+                         **dict(configs.plain_damping(K), delt=delt, strictly_linear=lin))
+            m, _, _ = make_ensemble_model(bs, E, cfg, device="cuda", nlon=nlon, nlat=nlat,
+                                          nmax=nmax, sigm=sigm)
+            stp = m.stepper()
+            sched = m._schedule(spd * max(days))
+            stp.set_timesteps(sorted({dt for dt, _ in sched}))
+            stp.set_forcing(frc_t=m._spec_forcing(torch.as_tensor(h, device="cuda"), True),
+                            per_member=True)
+            stp.load_zero()
+            snaps, done = {}, 0
+            for d in sorted(days):
+                upto = spd * d + m.cfg.inistp
+                stp.run(sched[done:upto], use_graph=True)
+                done = upto
+                torch.cuda.synchronize()
+                snaps[d] = (None if not stp.check_finite() else
+                            {"vor": stp.sa3[:, 0].to(torch.complex128),
+                             "div": stp.sa3[:, 1].to(torch.complex128),
+                             "t": stp.sa3[:, 2].to(torch.complex128),
+                             "pi": stp.sas[:, 0].to(torch.complex128)})
+            runs[name] = snaps
+            del m, stp
+        rec = {"members": E, "dt_s": delt, "strictly_linear": lin}
+        for d in sorted(days):
+            r = runs["fp64"][d]
+            for name in ("fp64_input_rounded", "fp32"):
+                x = runs[name][d]
+                if r is None or x is None:
+                    rec[f"{name}_day{d}"] = "non-finite"
+                    continue
+                rec[f"{name}_day{d}"] = {k: float(torch.linalg.norm(x[k] - r[k]) /
+                                                  torch.linalg.norm(r[k])) for k in r}
+        out[f"T{nmax}L{K}" + ("_strictly_linear" if lin else "_default")] = rec
     return out
 
 
@@ -449,6 +519,11 @@ def main():
         out = adjoint_measurement(torch, fd_dirs=args.fd_dirs, nsteps=args.adjoint_steps)
         print(json.dumps({"adjoint": out}), flush=True)
         return
+    if args.conditioning:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps({"conditioning": conditioning(torch)}), flush=True)
+        return
     if args.sweep:
         import torch
         torch.cuda.set_device(0)
@@ -510,8 +585,9 @@ def main():
     L = lib()
     sh = stream_handle(stp.stream)
     # kernel ids of lbm_stepper_launch in step order
-    kids = [4, 5, 6, 1, 2, 3] if args.precision == "fp32" else [0, 1, 2, 3]
-    names = (["idft", "alg", "fdft"] if args.precision == "fp32" else ["grid"]) + \
+    fp32s = args.precision != "fp64"          # FP32 state (fp32 and the bf16 modes)
+    kids = [4, 5, 6, 1, 2, 3] if fp32s else [0, 1, 2, 3]
+    names = (["idft", "alg", "fdft"] if fp32s else ["grid"]) + \
         ["anal", "implicit", "synth"]
     nk = len(kids)
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(nk + 1)]
@@ -560,28 +636,7 @@ def main():
     # ---- end to end through the public API, host buffers ----
     e2e = None
     if rank == 0:
-        days = args.steps / model.cfg.steps_per_day
-        m2, _ = build_model(E, args.precision, torch, days=days, seed=SEED + rank)
-        m2.stepper()
-        host_heat = torch.from_numpy(heats.astype(np.float64)).pin_memory()
-        warm = torch.empty(1, device="cuda")
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        dev_heat = host_heat.to("cuda", non_blocking=True)
-        m2.run(mjo_forcing=EnsembleForcing(dev_heat, device="cuda"), verbose=False)
-        out = {k: getattr(m2.ga, k).to("cpu") for k in ("u", "v", "t", "q", "ps")}
-        torch.cuda.synchronize()
-        t_e2e = time.perf_counter() - t0
-        nb_in = host_heat.numel() * host_heat.element_size()
-        nb_out = sum(x.numel() * x.element_size() for x in out.values())
-        e2e = {"value": E * args.steps / t_e2e, "unit": UNIT,
-               "h2d_bytes_per_step": nb_in / args.steps,
-               "d2h_bytes_per_step": nb_out / args.steps,
-               "seconds": t_e2e,
-               "note": "LBM.run of the ensemble from host heatings (H2D inside), "
-                       f"{args.steps} advancing + {m2.cfg.inistp} start-up steps, final "
-                       "grid state copied to host (D2H inside)"}
-        del m2
+        e2e = end_to_end(args, E, heats, torch)
 
     # ---- extras: accuracy vs FP64 and the plain single-member FP64 rate ----
     extras = {}
@@ -589,7 +644,7 @@ def main():
         extras = side_measurements(args, torch)
 
     if rank == 0:
-        p = 4 if args.precision == "fp32" else 8
+        p = 4 if fp32s else 8
         ab = algorithmic_bytes(E, p)
         top = int(np.argmax(kern_ms))
         peaks = {}
@@ -604,10 +659,11 @@ def main():
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32" if args.precision == "fp32" else "f64", "data": "synthetic",
+            "dtype": DTYPES[args.precision], "data": "synthetic",
             "config": {"workload": f"{E}-member T42L20 ensemble (solid-body basic state, "
                                    f"seeded elliptic heatings seed {SEED}+rank, plain "
-                                   "damping), FP32 state, fused stepper",
+                                   f"damping), FP32 state, fused stepper, Legendre analysis "
+                                   f"{LEGENDRE_NOTE[args.precision]}",
                        "members_per_gpu": E, "grid": "T42 128x64 Gaussian",
                        "levels": "L20 equal sigma", "dt_s": delt,
                        "l2": "inputs larger than L2 (per-step working set "
@@ -615,7 +671,7 @@ def main():
                        "parallelism": f"members sharded, {world} independent rank(s)"},
             "clocks": clk.summary(),
             "e2e": e2e,
-            "gpu_launches": nk * args.steps,
+            "gpu_launches": (nk + (1 if stp.legendre else 0)) * args.steps,
             "roofline": {"bound": "hbm", "kernel": names[top], "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": read_traffic(names[top], E),
@@ -635,32 +691,110 @@ def main():
         dist.destroy_process_group()
 
 
-def side_measurements(args, torch):
-    """FP32-vs-FP64 relative L2 per prognostic field after 10 and 30 days
-    (32 members of the bench's heatings; the FP64 path equals the numpy oracle
-    to 1e-10) and the plain single-member FP64 GPU rate that the batched rate
-    is compared with."""
-    out = {}
-    E = 32
+def end_to_end(args, E, heats, torch):
+    """The bench's steps through the public API with host buffers: the
+    pinned host heatings are copied to the device, LBM.run integrates the
+    ensemble (forcing analysis, state load, the steps, synthesis of the final
+    grid state) and the final grid state is copied into pinned host buffers
+    allocated beforehand, as a caller that reads every run's result keeps
+    them.  One untimed run first (kernel loading, allocator growth); the
+    timed run starts from the zero state again; a third run with
+    Config.phase_timing (device synchronised at phase boundaries) gives the
+    split by phase, reported beside the timed number."""
     from lbm_isca_gb300.ensemble import EnsembleForcing
-    worst = {}
-    for nday in (10, 30):
-        res = {}
-        for prec in ("fp64", "fp32"):
-            m, heats = build_model(E, prec, torch, days=nday)
-            m.run(mjo_forcing=EnsembleForcing(heats, device="cuda"), verbose=False)
-            a, _ = m.stepper().spectral_state()
-            res[prec] = {k: v.cpu().numpy() for k, v in a.items()}
-            del m
+    fields = ("u", "v", "t", "q", "ps")
+    days = args.steps / 72.0
+    m2, _ = build_model(E, args.precision, torch, days=days, seed=SEED)
+    host_heat = torch.from_numpy(heats.astype(np.float64)).pin_memory()
+    host_out = {k: torch.empty(tuple(getattr(m2.ga, k).shape), dtype=torch.float64,
+                               pin_memory=True) for k in fields}
+
+    def one_run(profile):
+        for st in (m2.ga, m2.gb):
+            for k in fields:
+                getattr(st, k).zero_()
+        m2.cfg.phase_timing = profile
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dev_heat = host_heat.to("cuda", non_blocking=True)
+        m2.run(mjo_forcing=EnsembleForcing(dev_heat, device="cuda"), verbose=False)
+        t1 = time.perf_counter()
+        for k in fields:
+            host_out[k].copy_(getattr(m2.ga, k), non_blocking=True)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        return t2 - t0, t2 - t1
+
+    one_run(False)
+    t_e2e, _ = one_run(False)
+    _, t_d2h = one_run(True)
+    phases = dict(m2.phases or {})
+    phases["d2h"] = t_d2h
+    nb_in = host_heat.numel() * host_heat.element_size()
+    nb_out = sum(x.numel() * x.element_size() for x in host_out.values())
+    del m2
+    return {"value": E * args.steps / t_e2e, "unit": UNIT,
+            "h2d_bytes_per_step": nb_in / args.steps,
+            "d2h_bytes_per_step": nb_out / args.steps,
+            "seconds": t_e2e,
+            "phases_s": phases,
+            "note": "LBM.run of the ensemble from pinned host heatings (H2D inside), "
+                    f"{args.steps} advancing + 2 start-up steps, final grid state copied "
+                    "to pinned host buffers (D2H inside); after one untimed run; "
+                    "phases_s from a further run synchronised at phase boundaries"}
+
+
+def accuracy_block(args, torch, E, days=(10, 30)):
+    """Relative L2 per prognostic field of the bench's precision against FP64
+    over every member of the timed ensemble (its heatings, seed 1) after 10
+    and 30 days: one run of each precision through the fused stepper, the
+    state taken at the end of day 10 (call 722) and of day 30 (call 2162);
+    packed spectral coefficients of all members (vor, div, T: every level;
+    pi), q' as its absolute maximum (it stays 0: no moisture forcing)."""
+    res = {}
+    for prec in ("fp64", args.precision):
+        m, heats = build_model(E, prec, torch, days=max(days))
+        stp = m.stepper()
+        sched = m._schedule(72 * max(days))
+        stp.set_timesteps(sorted({dt for dt, _ in sched}))
+        stp.set_forcing(frc_t=m._spec_forcing(torch.as_tensor(heats, device="cuda"), True),
+                        per_member=True)
+        stp.load_zero()
+        snaps, done = {}, 0
+        for d in sorted(days):
+            upto = 72 * d + m.cfg.inistp
+            stp.run(sched[done:upto], use_graph=True)
+            done = upto
+            torch.cuda.synchronize()
+            snaps[d] = {"vor": stp.sa3[:, 0].to(torch.complex128),
+                        "div": stp.sa3[:, 1].to(torch.complex128),
+                        "t": stp.sa3[:, 2].to(torch.complex128),
+                        "pi": stp.sas[:, 0].to(torch.complex128),
+                        "q": stp.sa3[:, 3].to(torch.complex128)}
+        if not stp.check_finite():
+            raise FloatingPointError(f"accuracy run in {prec} produced non-finite values")
+        res[prec] = snaps
+        del m, stp
+    out, worst = {}, {}
+    for d in sorted(days):
         rel = {}
         for k in ("vor", "div", "t", "pi"):
-            r, f = res["fp64"][k], res["fp32"][k]
-            rel[k] = float(np.linalg.norm(f - r) / np.linalg.norm(r))
-            worst[nday] = max(worst.get(nday, 0.0), rel[k])
-        rel["q_absmax"] = float(np.abs(res["fp32"]["q"]).max())
-        out[f"accuracy_fp32_vs_fp64_day{nday}"] = rel
-    out["accuracy_max_rel_l2"] = {f"day{n}": v for n, v in worst.items()}
-    out["accuracy_within_1e-5"] = {f"day{n}": bool(v <= 1e-5) for n, v in worst.items()}
+            r, f = res["fp64"][d][k], res[args.precision][d][k]
+            rel[k] = float(torch.linalg.norm(f - r) / torch.linalg.norm(r))
+            worst[d] = max(worst.get(d, 0.0), rel[k])
+        rel["q_absmax"] = float(res[args.precision][d]["q"].abs().max())
+        out[f"accuracy_vs_fp64_day{d}"] = rel
+    out["accuracy_max_rel_l2"] = {f"day{d}": v for d, v in worst.items()}
+    out["accuracy_within_1e-5"] = {f"day{d}": bool(v <= 1e-5) for d, v in worst.items()}
+    out["accuracy_members"] = E
+    return out
+
+
+def side_measurements(args, torch):
+    """FP32-vs-FP64 relative L2 per prognostic field after 10 and 30 days over
+    every member of the timed ensemble, and the plain single-member FP64 GPU
+    rate that the batched rate is compared with."""
+    out = accuracy_block(args, torch, args.members)
     # plain single-member FP64 GPU path
     m1, heats = build_model(1, "fp64", torch, days=1.0)
     stp = m1.stepper()

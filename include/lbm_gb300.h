@@ -252,6 +252,24 @@ int lbm_implicit_step_adjoint(int prec, const lbm_implicit_adj_args* a, void* st
  *   frc3 [Ef][4][NS][K], frcs [Ef][NS]: spectral forcing (NULL = none),
  *        Ef = E or 1 (frc_shared = 1)
  *   err [1] int: set nonzero when a non-finite value is produced
+ *   err_member [E] int or NULL: when given, entry e is also set nonzero when
+ *        member e produces a non-finite value, so that the host can name the
+ *        members that blew up (the reference's FloatingPointError,
+ *        model.py:245-247); the kernels only ever set these flags, the caller
+ *        clears them
+ *   legendre: 0 = the Legendre analysis on the FP32 FMA pipes; 3 or 6 = on
+ *        the tensor cores (tcgen05, FP32 mode only): af split into three
+ *        bfloat16 pieces, products summed in FP32 in tensor memory, 6 = the
+ *        six products down to third order (FP32-level accuracy), 3 = the
+ *        three products of a two-way split (about 16 bits)
+ *   tc_anal: table image of the tensor-core analysis (legendre != 0), 16-byte
+ *        aligned: for m = 0..N, for each step s of 16 latitudes, the tables
+ *        P, H and nn1a P (in that order), each as three bfloat16 pieces
+ *        (b0 = bf16(x), b1 = bf16(x - b0), b2 = bf16(x - b0 - b1), split from
+ *        FP64), each piece an NB(m) x 16 tile (NB(m) = N + 1 - m rounded up to
+ *        16; rows n - m, zero past N) whose element (r, kk) sits at byte
+ *        (r / 8) 256 + (kk / 8) 128 + (r % 8) 16 + (kk % 8) 2; needs nlat a
+ *        multiple of 16 and kmax even
  * sf, af and grid9 must be 16-byte aligned (LBM_ERR_ARG otherwise).
  * ==========================================================================*/
 enum {
@@ -272,6 +290,9 @@ typedef struct lbm_stepper_desc {
   void *sf, *sfs, *af, *afs, *tend, *tends;
   void *grid6, *grid9;
   int* err;
+  int* err_member;
+  int legendre;
+  const void* tc_anal;
 } lbm_stepper_desc;
 
 /* Per-step control.  dt: time step of this call; set: which operator set
@@ -396,7 +417,13 @@ int lbm_zonal_filter(int nlat, int nlon, int nk, double* x, int mode, void* stre
  *     carries over from an earlier call: the state in d is all there is.
  *   - Set-up: the first call on a device looks up the array's address with
  *     cudaGetSymbolAddress, with that device current, and keeps it.  Make the
- *     first call on each device before any stream capture begins.
+ *     first call on each device before any stream capture begins.  The kept
+ *     address belongs to the device's primary context, the one the CUDA
+ *     runtime uses: only callers that run under that context are supported,
+ *     and a device reset (cudaDeviceReset) after the first call leaves the
+ *     kept address invalid, so do not call this entry point after one.
+ *   - nlon must be 64, 128 or 256 and every size positive (LBM_ERR_ARG);
+ *     the whole descriptor is checked before the area is cleared.
  *   - The area is shared by every call on a device: two calls whose work
  *     overlaps on the GPU (different streams, or different host threads with
  *     no ordering between them) race on it and give wrong results.  Order

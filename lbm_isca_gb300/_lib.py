@@ -77,7 +77,8 @@ class StepperDesc(C.Structure):
                                      "tmtx", "minv", "vdiff", "frc3", "frcs", "dft", "sa3", "sas",
                                      "sb3", "psa", "psb", "sf", "sfs", "af", "afs", "tend",
                                      "tends", "grid6", "grid9")]
-                + [("err", C.POINTER(I32))])
+                + [("err", C.POINTER(I32)), ("err_member", C.POINTER(I32)),
+                   ("legendre", I32), ("tc_anal", VP)])
 
 
 class StepCtl(C.Structure):

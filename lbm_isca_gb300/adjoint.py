@@ -40,9 +40,8 @@ import types
 import numpy as np
 import torch
 
-from . import _lib
-from ._lib import ImplicitAdjArgs, TendAdjArgs, check, lib, ptr
-from .backend import stream_handle, to_device
+from . import ops as _ops
+from .backend import to_device
 from .checkpoint import schedule as binomial_schedule
 from .configs import response_box
 from .constants import EPSVT, KAPPA, RAIR
@@ -293,36 +292,17 @@ class TimeStep:
     def _tend_adjoint_kernel(self, ga, a_o):
         sp, vg, bs = self.sp, self.vg, self.m.bst
         J, I, K = sp.nlat, sp.nlon, vg.kmax
-        f64 = dict(device=sp.device, dtype=torch.float64)
-        lead = self._lead()
-        out = {k: torch.empty(lead + (J, I, K), **f64) for k in ("u", "v", "t", "q", "vor", "div")}
-        out["pix"] = torch.empty(lead + (J, I), **f64)
-        out["piy"] = torch.empty(lead + (J, I), **f64)
-        keep = []
-
-        def c(x):
-            t = x.contiguous()
-            keep.append(t)
-            return ptr(t)
-
-        a = TendAdjArgs()
-        a.nmem, a.nlat, a.nlon, a.kmax = self.nmem, J, I, K
-        a.kappa, a.epsvt, a.rair = KAPPA, EPSVT, RAIR
-        a.dsig, a.sigm, a.alpha, a.w3, a.wP = (c(vg.dsig), c(vg.sigm), c(vg.alpha), c(vg.w3),
-                                               c(vg.wP))
-        a.cpg, a.ww, a.tmtx, a.tref = c(vg.cpg), c(vg.ww), c(vg.tmtx), c(vg.tbar)
-        a.ub, a.vb, a.tb, a.qb, a.tvb = c(bs.u), c(bs.v), c(bs.t), c(bs.q), c(bs.tv)
-        a.absvor, a.divb, a.x5b, a.sdotb = c(bs.absvor), c(bs.div), c(bs.x5), c(bs.sdot)
-        a.pixb, a.piyb = c(bs.pix), c(bs.piy)
-        if not self.linear:
-            a.u0, a.v0 = c(ga.u), c(ga.v)
+        named = {"dsig": vg.dsig, "sigm": vg.sigm, "alpha": vg.alpha, "w3": vg.w3, "wP": vg.wP,
+                 "cpg": vg.cpg, "ww": vg.ww, "tmtx": vg.tmtx, "tref": vg.tbar, "ub": bs.u,
+                 "vb": bs.v, "tb": bs.t, "qb": bs.q, "tvb": bs.tv, "absvor": bs.absvor,
+                 "divb": bs.div, "x5b": bs.x5, "sdotb": bs.sdot, "pixb": bs.pix,
+                 "piyb": bs.piy, "u0": None if self.linear else ga.u,
+                 "v0": None if self.linear else ga.v}
         for k in ("fu", "fv", "ke", "gt", "xu", "xv", "g", "yu", "yv", "gt_pi"):
-            setattr(a, "a_" + k, c(a_o[k]))
-        for k in ("u", "v", "t", "q", "vor", "div", "pix", "piy"):
-            setattr(a, "a_" + k, ptr(out[k]))
-        check(lib().lbm_tendency_grid_adjoint(_lib.LBM_F64, a, stream_handle()),
-              "lbm_tendency_grid_adjoint")
-        return out
+            named["a_" + k] = a_o[k].to(torch.float64)
+        outs = torch.ops.lbm_gb300.tendency_grid_adjoint(
+            [named[k] for k in _ops.TADJ_INPUTS], self.nmem, J, I, K, [KAPPA, EPSVT, RAIR])
+        return {k[2:]: t for k, t in zip(_ops.TADJ_OUTPUTS, outs)}
 
     def adjoint_tendencies(self, ga, aw):
         """Transpose of ``tangent_tendencies``: adjoints of the five spectral
@@ -347,25 +327,13 @@ class TimeStep:
         integ.vdiff.prepare(dt)
         dmp = integ.dmp
         keys = ("vor", "div", "t", "pi", "q")
-        an = {k: an[k].to(torch.complex128).contiguous() for k in keys}
-        ap = {k: torch.empty_like(an[k]) for k in keys}
-        aw = {k: torch.empty_like(an[k]) for k in keys}
-        keep = [vg.ww.contiguous(), vg.tmtx.contiguous(), vg.gg.contiguous(),
-                vg.dsig.contiguous()]
-        a = ImplicitAdjArgs()
-        a.nmem, a.nmax, a.kmax, a.dt = self.nmem, sp.nmax, vg.kmax, float(dt)
-        a.lap, a.kv, a.kd, a.ktt, a.kq = (ptr(sp.laplace), ptr(dmp.kv), ptr(dmp.kd),
-                                          ptr(dmp.ktt), ptr(dmp.kq))
-        a.ww, a.tmtx, a.gg, a.dsig = (ptr(x) for x in keep)
-        a.minv = ptr(integ.semi.minv)
         mv = integ.vdiff.minv
-        a.vd_vor, a.vd_div, a.vd_t, a.vd_q = (ptr(mv.get(n)) for n in ("vor", "div", "t", "q"))
-        a.an_vor, a.an_div, a.an_t, a.an_pi, a.an_q = (ptr(an[k]) for k in keys)
-        a.ap_vor, a.ap_div, a.ap_t, a.ap_pi, a.ap_q = (ptr(ap[k]) for k in keys)
-        a.aw_vor, a.aw_div, a.aw_t, a.aw_pi, a.aw_q = (ptr(aw[k]) for k in keys)
-        check(lib().lbm_implicit_step_adjoint(_lib.LBM_F64, a, stream_handle()),
-              "lbm_implicit_step_adjoint")
-        return ap, aw
+        opsl = [sp.laplace, dmp.kv, dmp.kd, dmp.ktt, dmp.kq, vg.ww, vg.tmtx, vg.gg, vg.dsig,
+                integ.semi.minv] + [mv.get(n) for n in ("vor", "div", "t", "q")]
+        outs = torch.ops.lbm_gb300.implicit_step_adjoint(
+            opsl, [an[k].to(torch.complex128) for k in keys], self.nmem, sp.nmax, vg.kmax,
+            float(dt))
+        return dict(zip(keys, outs[:5])), dict(zip(keys, outs[5:]))
 
     def adjoint(self, ga, gb, gc_ps, a_ga, a_gb, dt, start):
         """Transpose of ``tangent``: adjoints of (ga', gb') -> adjoints of

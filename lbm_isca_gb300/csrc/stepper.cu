@@ -49,6 +49,9 @@ template <typename R> struct SD {
   C2<R> *sf, *sfs, *af, *afs, *tend, *tends;
   float *grid6, *grid9;
   int* err;
+  int* err_member;
+  int legendre;                          // 0 FMA; 3 or 6: tensor-core products
+  const unsigned char* tc_anal;          // table image of k_anal_tc
 };
 
 template <typename R> SD<R> make_sd(const lbm_stepper_desc& d) {
@@ -73,6 +76,9 @@ template <typename R> SD<R> make_sd(const lbm_stepper_desc& d) {
   s.tend = (C2<R>*)d.tend; s.tends = (C2<R>*)d.tends;
   s.grid6 = (float*)d.grid6; s.grid9 = (float*)d.grid9;
   s.err = d.err;
+  s.err_member = d.err_member;
+  s.legendre = d.legendre;
+  s.tc_anal = (const unsigned char*)d.tc_anal;
   return s;
 }
 
@@ -366,7 +372,9 @@ template <typename R> struct PairRows {
 // two partial groups).
 template <int NC> LBM_HD int anal_groups(int N) { return (N + 2 + NC - 1) / NC + 1; }
 
-template <typename R, int NC, int KC>
+// SURF: only the surface part (tends), for the tensor-core analysis, which
+// computes the level part (k_anal_tc).
+template <typename R, int NC, int KC, bool SURF = false>
 __global__ void k_anal(SD<R> d) {
   const int p = blockIdx.x, e = blockIdx.y, kc = blockIdx.z;
   const int J = d.J, K = d.K, N = d.N, M = d.M, JH = J / 2;
@@ -403,6 +411,8 @@ __global__ void k_anal(SD<R> d) {
       th[jh * TS + sl] = row >= 0 ? d.symh[(size_t)row * JH + jh] : R(0);
     }
   }
+  const int nm = pr.L2 ? 2 : 1;
+  if constexpr (!SURF) {
   const int k = tid % KC, g = tid / KC;
   const bool active = (k < kn) && (g < G1 + G2);
   const int mi = (g < G1) ? 0 : 1;
@@ -415,7 +425,6 @@ __global__ void k_anal(SD<R> d) {
     for (int a = 0; a < 9; ++a) acc[i][a] = cmk<R>(0, 0);
   const size_t jmK = (size_t)J * K;
   const C2<R>* afe = d.af + (size_t)e * M * jmK * AF_N;
-  const int nm = pr.L2 ? 2 : 1;
   const int rowlen = kn * AF_N;                 // complex values per (m, latitude) row
   const int rowst = KC * AF_N;                  // row stride in the buffer
   const size_t rawbuf = (size_t)2 * AN_JC * 2 * rowst;
@@ -507,6 +516,7 @@ __global__ void k_anal(SD<R> d) {
       te[(3 * NS + idx) * K + k0 + k] = qq;
     }
   }
+  }  // !SURF
   // surface: wt_pi and pi(t - dt), one thread per row (first level chunk only)
   if (kc != 0) return;
   __syncthreads();
@@ -713,7 +723,10 @@ __global__ void __launch_bounds__(IM_THREADS) k_implicit(SD<R> d, R dt, int set,
       const bool fin = isfinite(nV.x) && isfinite(nV.y) && isfinite(nD.x) && isfinite(nD.y) &&
                        isfinite(nT.x) && isfinite(nT.y) && isfinite(nQ.x) && isfinite(nQ.y) &&
                        isfinite(npi.x) && isfinite(npi.y);
-      if (!fin) atomicOr(d.err, 1);
+      if (!fin) {
+        atomicOr(d.err, 1);
+        if (d.err_member) atomicOr(d.err_member + e, 1);
+      }
     }
     // column sums for sigma-dot of the next step
     __syncthreads();
@@ -992,6 +1005,7 @@ __global__ void k_ps_flush(SD<R> d, int ps_mode) {
 
 }  // namespace lbm
 #include "grid_split.cuh"
+#include "legendre_tc.cuh"
 namespace lbm {
 
 // ---- launch configuration ------------------------------------------------------
@@ -1030,10 +1044,15 @@ template <typename R, int KC> void launch_anal(const SD<R>& d, cudaStream_t st, 
   const size_t sm2 = sizeof(R) * 2 * ((size_t)NC * G + 1) * JH + 16 +
                      sizeof(C2<R>) * (size_t)2 * JH * 2 * 2;
   if (sm2 > sm) sm = sm2;
-  if (attrs)
+  if (attrs) {
     cudaFuncSetAttribute(k_anal<R, NC, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  else
+    cudaFuncSetAttribute(k_anal<R, NC, KC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sm);
+  } else if (d.legendre && sizeof(R) == 4) {
+    k_anal<R, NC, KC, true><<<dim3(NP, d.E, 1), nt, sm, st>>>(d);
+  } else {
     k_anal<R, NC, KC><<<dim3(NP, d.E, (d.K + KC - 1) / KC), nt, sm, st>>>(d);
+  }
 }
 template <typename R> void run_anal(const SD<R>& d, cudaStream_t st, bool attrs) {
   if (anal_kc<R>(d.N) == Cfg<R>::KCA) launch_anal<R, Cfg<R>::KCA>(d, st, attrs);
@@ -1109,7 +1128,16 @@ template <typename R, int I> int launch_step(const SD<R>& d, const lbm_step_ctl&
     if (only < 0 || only == 0)
       k_grid<R, I, KB, NT><<<dim3(d.J, d.E), NT, gsm, st>>>(d, c.ps_mode);
   }
-  if (only < 0 || only == 1) run_anal<R>(d, st, false);
+  if (only < 0 || only == 1) {
+    if constexpr (sizeof(R) == 4) {
+      if (d.legendre) {
+        const AtcPlan pl = atc_plan(d.E, d.J, d.K, d.N);
+        k_anal_tc<<<persistent_grid((const void*)k_anal_tc, ATC_THREADS, pl.smem, pl.nunits),
+                    ATC_THREADS, pl.smem, st>>>(d, d.tc_anal, pl, d.legendre);
+      }
+    }
+    run_anal<R>(d, st, false);
+  }
   if (only < 0 || only == 2)
     k_implicit<R><<<dim3(NP, d.E), IM_THREADS, impl_smem<R>(d.K), st>>>(d, R(c.dt), c.set,
                                                                          c.ra_mode);
@@ -1135,6 +1163,13 @@ template <typename R, int I> void set_attrs(const SD<R>& d) {
                          (int)GridSmem<R, I, KB, NT>::bytes(d.M));
   }
   run_anal<R>(d, nullptr, true);
+  if constexpr (sizeof(R) == 4) {
+    if (d.legendre) {
+      const AtcPlan pl = atc_plan(d.E, d.J, d.K, d.N);
+      cudaFuncSetAttribute(k_anal_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
+      persistent_grid((const void*)k_anal_tc, ATC_THREADS, pl.smem, 1);
+    }
+  }
   cudaFuncSetAttribute(k_implicit<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)impl_smem<R>(d.K));
   cudaFuncSetAttribute(k_synth<R, Cfg<R>::JG, Cfg<R>::KCS, Cfg<R>::SHV>,
@@ -1157,6 +1192,15 @@ template <typename R> int validate(const SD<R>& d) {
   // 16-byte copies and bulk prefetches read sf, af and grid9
   auto a16 = [](const void* p) { return ((uintptr_t)p & 15) == 0; };
   if (!a16(d.sf) || !a16(d.af) || (sizeof(R) == 4 && !a16(d.grid9))) return LBM_ERR_ARG;
+  if (d.legendre) {
+    // tensor-core analysis: FP32 state, 16-latitude steps, 16-byte af rows,
+    // at most 256 table rows, the plan within shared memory
+    if (sizeof(R) != 4 || (d.legendre != 3 && d.legendre != 6) || !d.tc_anal ||
+        (d.J % 16) || (d.K & 1) || d.M > 256 ||
+        atc_plan(d.E, d.J, d.K, d.N).smem > 227 * 1024 ||
+        ((uintptr_t)d.tc_anal & 15))
+      return LBM_ERR_ARG;
+  }
   if (sizeof(R) == 4 &&
       (idft_smem(d.I, d.M) > 227 * 1024 ||
        sizeof(float) * (size_t)fdft_plan(d.I, d.M, d.K).total > 227 * 1024))
@@ -1283,7 +1327,10 @@ static void noalloc_layout(const lbm_stepper_desc& d, size_t off[8], double* nee
 
 // Device address of the scratch area on the current device.  The first call
 // on a device looks it up with cudaGetSymbolAddress (with that device
-// current) and keeps it; later calls reuse it.
+// current) and keeps it; later calls reuse it.  The address belongs to the
+// device's primary context (the one the CUDA runtime uses): a caller running
+// under another context of its own, or one that resets the device after the
+// first call, would be handed an address that is no longer valid there.
 static int noalloc_base(void** out) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES)
@@ -1300,6 +1347,9 @@ static int noalloc_base(void** out) {
 
 template <typename R> int run_noalloc(const lbm_stepper_desc& w, const lbm_step_ctl* ctl,
                                       int nsteps, size_t clear, cudaStream_t st) {
+  // the full argument check runs before the clear, capturing or not
+  const int vrc = validate(make_sd<R>(w));
+  if (vrc) return vrc;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   cudaStreamIsCapturing(st, &cs);
   if (cs == cudaStreamCaptureStatusNone) {
@@ -1418,9 +1468,11 @@ int lbm_stepper_run_noalloc(const lbm_stepper_desc* d, const lbm_step_ctl* ctl, 
                             void* stream) {
   if (!d || !ctl || nsteps < 0 || (d->prec != LBM_F64 && d->prec != LBM_F32)) return LBM_ERR_ARG;
   if (d->nmem < 1 || d->nlat < 2 || d->nmax < 1 || d->kmax < 1) return LBM_ERR_ARG;
+  if (d->nlon != 64 && d->nlon != 128 && d->nlon != 256) return LBM_ERR_ARG;
   size_t off[8];
   double need = 0.0;
   noalloc_layout(*d, off, &need);
+  if (!(need > 0.0)) return LBM_ERR_ARG;
   if (need > (double)LBM_NOALLOC_SCRATCH_BYTES) return LBM_ERR_SCRATCH;
   for (int s = 0; s < nsteps; ++s)
     if (ctl[s].set < 0 || ctl[s].set >= d->nsets || ctl[s].ps_mode < 0 || ctl[s].ps_mode > 2 ||

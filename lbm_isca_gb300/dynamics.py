@@ -17,9 +17,8 @@ from __future__ import annotations
 import numpy as np
 import torch
 
-from . import _lib
-from ._lib import TendGridArgs, check, lib, ptr
-from .backend import to_device, stream_handle
+from . import ops as _ops
+from .backend import to_device
 from .constants import EPSVT, KAPPA, OMEGA, RAIR
 
 
@@ -92,55 +91,39 @@ class Dynamics:
         tangent-linear kinetic energy u0 u + v0 v in place of 0.5 (u^2 + v^2)."""
         sp, vg, bs = self.sp, self.vg, self.bs
         dev = sp.device
-        u, v = st.u.contiguous(), st.v.contiguous()
+        u = st.u
         batched = u.dim() == 4
         E = u.shape[0] if batched else 1
         J, I, K = sp.nlat, sp.nlon, vg.kmax
-        f64 = dict(device=dev, dtype=torch.float64)
-        shp3 = u.shape
+        shp3 = tuple(u.shape)
         shp2 = shp3[:-1]
-        out = {k: torch.empty(shp3, **f64) for k in
-               ("fu", "fv", "ke", "gt", "xu", "xv", "g", "yu", "yv")}
-        out["gt_pi"] = torch.empty(shp2, **f64)
-        out["omega"] = torch.empty(shp3, **f64) if want_omega else None
-        out["sdot"] = torch.empty(shp2 + (K + 1,), **f64)
-        keep = []
-
-        def c(x):
-            t = x.contiguous()
-            keep.append(t)
-            return ptr(t)
 
         def frc(x, full_shape):
             if x is None:
                 return None, 0
-            t = to_device(x, dev).contiguous()
-            keep.append(t)
+            t = to_device(x, dev)
             per = int(np.prod(full_shape[1:])) if batched else 0
             stride = per if (batched and t.dim() == len(full_shape)) else 0
-            return ptr(t), stride
+            return t, stride
 
-        a = TendGridArgs()
-        a.nmem, a.nlat, a.nlon, a.kmax = E, J, I, K
-        a.strictly_linear = int(self.strictly_linear)
-        a.kappa, a.epsvt, a.rair = KAPPA, EPSVT, RAIR
-        tref = vg.tbar
-        a.dsig, a.sigm, a.alpha, a.w3, a.wP = (c(vg.dsig), c(vg.sigm), c(vg.alpha), c(vg.w3),
-                                               c(vg.wP))
-        a.cpg, a.sig, a.ww, a.tmtx, a.tref = c(vg.cpg), c(vg.sig), c(vg.ww), c(vg.tmtx), c(tref)
-        a.ub, a.vb, a.tb, a.qb, a.tvb = c(bs.u), c(bs.v), c(bs.t), c(bs.q), c(bs.tv)
-        a.absvor, a.divb, a.x5b, a.sdotb = c(bs.absvor), c(bs.div), c(bs.x5), c(bs.sdot)
-        a.pixb, a.piyb, a.psb = c(bs.pix), c(bs.piy), c(bs.ps)
-        a.u, a.v, a.t, a.q = c(u), c(v), c(st.t), c(st.q)
-        a.vor, a.div, a.pix, a.piy, a.ps = c(vor), c(div), c(pix), c(piy), c(st.ps)
-        a.frc_t, a.frc_t_stride = frc(frc_t, shp3)
-        a.frc_ps, a.frc_ps_stride = frc(frc_ps, shp2)
-        a.frc_q, a.frc_q_stride = frc(frc_q, shp3)
-        for k in ("fu", "fv", "ke", "gt", "xu", "xv", "g", "yu", "yv", "gt_pi", "omega", "sdot"):
-            setattr(a, k, ptr(out[k]))
-        if lin is not None:
-            a.lin_u, a.lin_v = c(lin[0]), c(lin[1])
-        check(lib().lbm_tendency_grid(_lib.LBM_F64, a, stream_handle()), "lbm_tendency_grid")
+        ft, ft_s = frc(frc_t, shp3)
+        fp, fp_s = frc(frc_ps, shp2)
+        fq, fq_s = frc(frc_q, shp3)
+        named = {"dsig": vg.dsig, "sigm": vg.sigm, "alpha": vg.alpha, "w3": vg.w3, "wP": vg.wP,
+                 "cpg": vg.cpg, "sig": vg.sig, "ww": vg.ww, "tmtx": vg.tmtx, "tref": vg.tbar,
+                 "ub": bs.u, "vb": bs.v, "tb": bs.t, "qb": bs.q, "tvb": bs.tv,
+                 "absvor": bs.absvor, "divb": bs.div, "x5b": bs.x5, "sdotb": bs.sdot,
+                 "pixb": bs.pix, "piyb": bs.piy, "psb": bs.ps, "u": u, "v": st.v, "t": st.t,
+                 "q": st.q, "vor": vor, "div": div, "pix": pix, "piy": piy, "ps": st.ps,
+                 "frc_t": ft, "frc_ps": fp, "frc_q": fq,
+                 "lin_u": None if lin is None else lin[0],
+                 "lin_v": None if lin is None else lin[1]}
+        outs = torch.ops.lbm_gb300.tendency_grid(
+            [named[k] for k in _ops.TEND_INPUTS], E, J, I, K, int(self.strictly_linear),
+            [KAPPA, EPSVT, RAIR], [ft_s, fp_s, fq_s], bool(want_omega))
+        out = dict(zip(_ops.TEND_OUTPUTS, outs))
+        if not want_omega:
+            out["omega"] = None
         return out
 
     def tendencies(self, st, frc_t=None, frc_vor=None, frc_div=None, frc_ps=None,

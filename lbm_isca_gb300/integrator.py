@@ -15,9 +15,8 @@ from __future__ import annotations
 import numpy as np
 import torch
 
-from . import _lib
-from ._lib import ImplicitArgs, check, lib, ptr
-from .backend import asnumpy, stream_handle
+from . import ops as _ops
+from .backend import asnumpy
 from .constants import S2D
 
 
@@ -84,12 +83,7 @@ class Damping:
 
 def batched_inverse(a):
     """FP64 batched inverse on the device (Gauss-Jordan, partial pivoting)."""
-    a = a.contiguous().to(torch.float64)
-    B, n, _ = a.shape
-    out = torch.empty_like(a)
-    info = torch.zeros(B, dtype=torch.int32, device=a.device)
-    check(lib().lbm_batched_inverse(B, n, ptr(a), ptr(out), ptr(info), stream_handle()),
-          "lbm_batched_inverse")
+    out, info = torch.ops.lbm_gb300.batched_inverse(a.contiguous().to(torch.float64))
     if int(info.max()) != 0:
         raise np.linalg.LinAlgError("singular matrix in batched inverse")
     return out
@@ -109,12 +103,8 @@ class SemiImplicit:
         dt = float(dt)
         if dt not in self._cache:
             sp, vg, dmp = self.sp, self.vg, self.dmp
-            M, K = sp.nmax + 1, vg.kmax
-            mats = torch.empty((M, K, K), device=sp.device, dtype=torch.float64)
-            check(lib().lbm_gravity_wave_matrices(
-                sp.nmax, K, dt, ptr(sp.laplace), ptr(dmp.ktt), ptr(dmp.kd),
-                ptr(vg.whmtx.contiguous()), ptr(vg.gcmtx.contiguous()), ptr(mats),
-                stream_handle()), "lbm_gravity_wave_matrices")
+            mats = torch.ops.lbm_gb300.gravity_wave_matrices(
+                sp.laplace, dmp.ktt, dmp.kd, vg.whmtx, vg.gcmtx, dt)
             minv = batched_inverse(mats)
             cond = np.array([np.linalg.cond(x) for x in asnumpy(mats)])
             self._cache[dt] = (mats, minv, cond)
@@ -222,19 +212,10 @@ class Integrator:
         K = vg.kmax
         batched = pv["vor"].dim() == 4
         E = pv["vor"].shape[0] if batched else 1
-        out = {k: torch.empty_like(pv[k]) for k in keys}
-        a = ImplicitArgs()
-        a.nmem, a.nmax, a.kmax, a.dt = E, sp.nmax, K, float(dt)
-        keep = [vg.ww.contiguous(), vg.tmtx.contiguous(), vg.gg.contiguous(),
-                vg.dsig.contiguous()]
-        a.lap, a.kv, a.kd, a.ktt, a.kq = (ptr(sp.laplace), ptr(dmp.kv), ptr(dmp.kd),
-                                          ptr(dmp.ktt), ptr(dmp.kq))
-        a.ww, a.tmtx, a.gg, a.dsig = (ptr(x) for x in keep)
-        a.minv = ptr(self.semi.minv)
         mv = self.vdiff.minv
-        a.vd_vor, a.vd_div, a.vd_t, a.vd_q = (ptr(mv.get(n)) for n in ("vor", "div", "t", "q"))
-        a.p_vor, a.p_div, a.p_t, a.p_pi, a.p_q = (ptr(pv[k]) for k in keys)
-        a.w_vor, a.w_div, a.w_t, a.w_pi, a.w_q = (ptr(tv[k]) for k in keys)
-        a.n_vor, a.n_div, a.n_t, a.n_pi, a.n_q = (ptr(out[k]) for k in keys)
-        check(lib().lbm_implicit_step(_lib.LBM_F64, a, stream_handle()), "lbm_implicit_step")
-        return out
+        opsl = [sp.laplace, dmp.kv, dmp.kd, dmp.ktt, dmp.kq, vg.ww, vg.tmtx, vg.gg, vg.dsig,
+                self.semi.minv] + [mv.get(n) for n in ("vor", "div", "t", "q")]
+        new = torch.ops.lbm_gb300.implicit_step(opsl, [pv[k] for k in keys],
+                                                [tv[k] for k in keys], E, sp.nmax, K,
+                                                float(dt))
+        return dict(zip(keys, new))

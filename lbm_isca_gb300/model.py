@@ -81,9 +81,14 @@ class Config:
     nmem: int = 1
     device: str = "auto"
     # --- GB300 path ----------------------------------------------------------
-    precision: str = "fp64"       # "fp64" | "fp32": working precision of the step
+    precision: str = "fp64"       # "fp64" | "fp32" | "bf16x3" | "bf16split": working
+                                  # precision of the step; the bf16 modes keep the FP32
+                                  # state and run the Legendre analysis on the tensor
+                                  # cores (3-way bf16 split, 6 or 3 products)
     fused: bool = True            # fused ensemble stepper (False: general loop)
     use_graph: bool = True        # replay steady-state steps as CUDA graphs
+    phase_timing: bool = False    # fused run: seconds per phase in LBM.phases
+                                  # (synchronises the device at phase boundaries)
 
     @property
     def steps_per_day(self):
@@ -129,6 +134,8 @@ class LBM:
         self.istep = 0
         self._stepper = None
         self._last_top = None
+        self.phases = None
+        self._phase_t = None
 
     @property
     def device(self):
@@ -216,11 +223,15 @@ class LBM:
         if verbose:
             print(f"  backend: {self.device}", flush=True)
         sched = self._schedule(nsteps)
+        self.phases = {} if cfg.phase_timing else None
+        if self.phases is not None:
+            torch.cuda.synchronize()
+            self._phase_t = _time.perf_counter()
         nonzero = any(bool((getattr(st, k) != 0).any()) for st in (self.ga, self.gb)
                       for k in ("u", "v", "t", "q", "ps"))
         if cfg.fused and (writer is None or not nonzero):
             self._run_fused(sched, mjo_forcing, steady_forcing, verbose, progress_every, t0,
-                            writer=writer)
+                            writer=writer, nonzero=nonzero)
         else:
             self._run_general(sched, mjo_forcing, steady_forcing, writer, verbose,
                               progress_every, t0)
@@ -350,7 +361,31 @@ class LBM:
         return {"psi": psi, "chi": chi, "u": u, "v": v, "w": o["omega"], "t": t, "z": z,
                 "p": ps}
 
-    def _run_fused(self, sched, mjo_forcing, sf, verbose, progress_every, t0, writer=None):
+    def _mark(self, name):
+        """Add the seconds since the previous mark to phase `name` (only with
+        Config.phase_timing; the device is synchronised first so that the
+        phase's GPU work is counted in it)."""
+        if self.phases is None:
+            return
+        torch.cuda.synchronize()
+        now = _time.perf_counter()
+        self.phases[name] = self.phases.get(name, 0.0) + (now - self._phase_t)
+        self._phase_t = now
+
+    def _blew_up(self, stp, a, b):
+        """FloatingPointError of the fused loop (model.py:245-247 raises at the
+        step itself): the device flags are read at day boundaries and at the
+        end of a run, so the message names the window of calls since the last
+        clean check and the members whose flags are set."""
+        bad = stp.bad_members()
+        who = (f"member{'s' if len(bad) > 1 else ''} {', '.join(map(str, bad))}"
+               if self.batched else "the model")
+        raise FloatingPointError(
+            f"model blew up at a step between {a + 1} and {b} of this run "
+            f"(t <= {self.time / 86400:.2f} d): non-finite values in {who}")
+
+    def _run_fused(self, sched, mjo_forcing, sf, verbose, progress_every, t0, writer=None,
+                   nonzero=True):
         cfg = self.cfg
         stp = self.stepper()
         stp.set_timesteps(sorted({dt for dt, _ in sched}))
@@ -367,8 +402,6 @@ class LBM:
             stp.set_forcing(frc_vor=fv, frc_div=fd, frc_t=ft, frc_pi=fp, per_member=per)
 
         first = 0
-        nonzero = any(bool((getattr(s, k) != 0).any()) for s in (self.ga, self.gb)
-                      for k in ("u", "v", "t", "q", "ps"))
         if nonzero:
             # forward start from an arbitrary grid state: one general step
             dt, start = sched[0]
@@ -390,19 +423,27 @@ class LBM:
             src = interp.next() if interp is not None else mjo_forcing.step()
             if src is not last_src[0]:
                 last_src[0] = src
+                self._mark("steps")
                 install(src if interp is not None else self._spec_forcing(src, True))
+                self._mark("forcing")
 
         self._last_top = None
         advanced = 1 if (first == 1 and not sched[0][1]) else 0
         if first >= len(sched):
             return
-        self._load_stepper(stp)
+        self._mark("setup")
+        if nonzero or first:
+            self._load_stepper(stp)
+        else:
+            stp.load_zero()          # a zero state is zero in every representation
+        self._mark("load")
         spd = cfg.steps_per_day
         out_every = int(round(cfg.out_interval_days * spd))
         day_done, sampled = 0, False
         if writer is not None:
             stp.hist_begin()
         i = first
+        checked = first          # calls of this run known to be finite
         while i < len(sched):
             if writer is not None:
                 # history: one step per call, sampled around its kernels
@@ -426,15 +467,17 @@ class LBM:
                 if not start:
                     self.time += dt
                     advanced += 1
-                    if advanced % out_every == 0:
-                        day_done += 1
-                        fields = self._diagnostics_mean(*stp.hist_mean())
-                        _emit(writer, day_done, fields)
-                        stp.hist_reset()
-                    if advanced % spd == 0 and not stp.check_finite():
-                        raise FloatingPointError(
-                            f"model blew up at or before step {i} of this run "
-                            f"(t={self.time / 86400:.2f} d)")
+                # the blow-up check comes before the day's record is written,
+                # as in the reference's loop (model.py:245-277)
+                if (not start and advanced % spd == 0) or i == len(sched):
+                    if not stp.check_finite():
+                        self._blew_up(stp, checked, i)
+                    checked = i
+                if not start and advanced % out_every == 0:
+                    day_done += 1
+                    fields = self._diagnostics_mean(*stp.hist_mean())
+                    _emit(writer, day_done, fields)
+                    stp.hist_reset()
                 continue
             if mjo_forcing is not None:
                 # time-varying forcing: one .step() call per model step
@@ -458,13 +501,14 @@ class LBM:
                 if not start:
                     self.time += dt
                     advanced += 1
-            if i == len(sched) or advanced % spd == 0:
+            if i == len(sched) or (advanced and advanced % spd == 0):
                 if not stp.check_finite():
-                    raise FloatingPointError(
-                        f"model blew up at or before step {i} of this run "
-                        f"(t={self.time / 86400:.2f} d)")
+                    self._blew_up(stp, checked, i)
+                checked = i
             if (verbose and progress_every and advanced and advanced % progress_every == 0
                     and i < len(sched)):
                 self._unload_stepper(stp)
                 self._progress(t0)
+        self._mark("steps")
         self._unload_stepper(stp)
+        self._mark("unload")

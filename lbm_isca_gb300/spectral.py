@@ -20,9 +20,9 @@ from __future__ import annotations
 import numpy as np
 import torch
 
-from . import _lib
-from ._lib import LBM_F32, LBM_F64, check, lib, ptr
-from .backend import resolve, stream_handle, to_device
+from . import ops as _ops  # noqa: F401  (registers torch.ops.lbm_gb300.*)
+from ._lib import LBM_F32, LBM_F64, lib
+from .backend import resolve, to_device
 from .constants import ER, IMAX, JMAX, NMAX
 
 _PREC = {"fp64": (torch.float64, torch.complex128, LBM_F64),
@@ -49,15 +49,13 @@ class Spectral:
             raise ValueError(f"precision must be one of {list(_PREC)}")
         self.precision = precision
         self.rdtype, self.cdtype, self.prec_id = _PREC[precision]
-        L = lib()
+        lib()                                      # fails loudly without the library
         dev = self.device
         M, J = self.nmax + 1, self.nlat
-        st = stream_handle()
         f64 = dict(device=dev, dtype=torch.float64)
+        LO = torch.ops.lbm_gb300
         # --- Gaussian grid (FP64 on the device; spectral.py:58-61) ----------
-        mu = torch.empty(J, **f64)
-        gw = torch.empty(J, **f64)
-        check(L.lbm_gauss_legendre(J, ptr(mu), ptr(gw), st), "lbm_gauss_legendre")
+        mu, gw = LO.gauss_legendre(torch.empty(0, **f64), J)
         self.mu = mu.cpu().numpy()                 # host, like the reference
         self.gw = gw.cpu().numpy()
         self.lat = np.arcsin(self.mu)
@@ -65,10 +63,7 @@ class Spectral:
         coslat_h = np.sqrt(1.0 - self.mu ** 2)
         self.gwdel = self.gw / self.a / (1.0 - self.mu ** 2)
         # --- Legendre tables (FP64 on the device; spectral.py:93-154) -------
-        P = torch.empty((M, M, J), **f64)
-        H = torch.empty((M, M, J), **f64)
-        check(L.lbm_legendre_tables(self.nmax, J, ptr(mu), ptr(P), ptr(H), st),
-              "lbm_legendre_tables")
+        P, H = LO.legendre_tables(mu, self.nmax)
         self.pnm, self.hnm = P, H
         gw_d = gw
         gwdel_d = torch.as_tensor(self.gwdel, **f64)
@@ -93,8 +88,7 @@ class Spectral:
         self.im = torch.as_tensor(1j * n, device=dev, dtype=torch.complex128)
         mm, nn_ = np.meshgrid(np.arange(M), np.arange(M), indexing="ij")
         self.mask = nn_ >= mm
-        tw = torch.empty(2 * self.nlon, **f64)
-        check(L.lbm_fft_twiddles(self.nlon, ptr(tw), st), "lbm_fft_twiddles")
+        tw = torch.view_as_real(LO.fft_twiddles(torch.empty(0, **f64), self.nlon)).reshape(-1)
         self._tw64 = tw
         # working-precision copies used by the transform kernels
         rd = self.rdtype
@@ -155,38 +149,20 @@ class Spectral:
     # kernel wrappers
     # ------------------------------------------------------------------
     def _fwd(self, g4, jscale=None):
-        B, J, I, Cn = g4.shape
-        M = self.nmax + 1
-        four = torch.empty((B, M, J, Cn), device=self.device, dtype=self.cdtype)
-        check(lib().lbm_fourier_forward(self.prec_id, B, J, I, Cn, self.nmax, ptr(g4),
-                                        ptr(jscale), ptr(self._t["tw"]), ptr(four),
-                                        stream_handle()), "lbm_fourier_forward")
-        return four
+        return torch.ops.lbm_gb300.fourier_forward(g4.to(self.rdtype), jscale,
+                                                   self._t["tw"], self.nmax)
 
     def _inv(self, four, jscale=None):
-        B, M, J, Cn = four.shape
-        g = torch.empty((B, J, self.nlon, Cn), device=self.device, dtype=self.rdtype)
-        check(lib().lbm_fourier_inverse(self.prec_id, B, J, self.nlon, Cn, self.nmax,
-                                        ptr(four), ptr(jscale), ptr(self._t["tw"]), ptr(g),
-                                        stream_handle()), "lbm_fourier_inverse")
-        return g
+        return torch.ops.lbm_gb300.fourier_inverse(four.to(self.cdtype), jscale,
+                                                   self._t["tw"], self.nlon)
 
     def _anal(self, fa, ta, ima, fb=None, tb=None, imb=0, sb=1.0, nfac=None):
-        B, M, J, Cn = fa.shape
-        spec = torch.empty((B, M, M, Cn), device=self.device, dtype=self.cdtype)
-        check(lib().lbm_legendre_analysis(self.prec_id, B, self.nmax, J, Cn, ptr(fa), ptr(ta),
-                                          ima, ptr(fb), ptr(tb), imb, float(sb), ptr(nfac), 0,
-                                          ptr(spec), stream_handle()), "lbm_legendre_analysis")
-        return spec
+        return torch.ops.lbm_gb300.legendre_analysis(fa.to(self.cdtype), ta, int(ima), fb, tb,
+                                                     int(imb), float(sb), nfac)
 
     def _synth(self, sa, ta, ima, na=None, sbp=None, tb=None, imb=0, nb=None, sb=1.0):
-        B, M, _, Cn = sa.shape
-        four = torch.empty((B, M, self.nlat, Cn), device=self.device, dtype=self.cdtype)
-        check(lib().lbm_legendre_synthesis(self.prec_id, B, self.nmax, self.nlat, Cn, ptr(sa),
-                                           ptr(ta), ima, ptr(na), ptr(sbp), ptr(tb), imb,
-                                           ptr(nb), float(sb), ptr(four), stream_handle()),
-              "lbm_legendre_synthesis")
-        return four
+        return torch.ops.lbm_gb300.legendre_synthesis(sa.to(self.cdtype), ta, int(ima), na,
+                                                      sbp, tb, int(imb), nb, float(sb))
 
     def _ret_grid(self, g4, meta):
         return g4.reshape(self._out_shape(meta, self.nlat, self.nlon))

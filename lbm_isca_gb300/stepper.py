@@ -22,6 +22,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from . import ops as _ops
 from ._lib import StepCtl, StepperDesc, check, lib, ptr
 from .backend import stream_handle
 from .constants import EPSVT, KAPPA, RAIR
@@ -29,13 +30,45 @@ from .constants import EPSVT, KAPPA, RAIR
 VERT_ROWS = 12   # LBM_VERT_COUNT in include/lbm_gb300.h
 
 
+def tc_anal_image(P, H, nn1a, N):
+    """Table image of the tensor-core Legendre analysis (the tc_anal layout of
+    include/lbm_gb300.h): per m, per step of 16 latitudes, the tables P, H
+    and nn1a P over rows n = m..N padded to a multiple of 16, each split from
+    FP64 into three bfloat16 pieces (b0 = bf16(x), b1 = bf16(x - b0),
+    b2 = bf16(x - b0 - b1)), each piece one K-major tile of 8-row x 16-byte
+    core matrices.  P, H: [M][M][J] FP64 (any device); returns int16 words."""
+    J = P.shape[-1]
+    KS = J // 16
+    P = P.to(torch.float64)
+    tabs = (P, H.to(torch.float64), P * nn1a.to(torch.float64)[None, :, None])
+    out = []
+    for m in range(N + 1):
+        nr = N + 1 - m
+        nb = (nr + 15) // 16 * 16
+        T = torch.zeros((3, nb, J), device=P.device, dtype=torch.float64)
+        for t in range(3):
+            T[t, :nr] = tabs[t][m, m:, :]
+        pieces, r = [], T
+        for _ in range(3):
+            b = r.to(torch.bfloat16)
+            pieces.append(b.view(torch.int16))
+            r = r - b.to(torch.float64)
+        x = torch.stack(pieces, 1)                        # [t][p][nb][J]
+        x = x.reshape(3, 3, nb // 8, 8, KS, 2, 8)          # [t][p][rg][r8][s][kc][k8]
+        out.append(x.permute(4, 0, 1, 2, 5, 3, 6).reshape(-1))
+    return torch.cat(out).contiguous()
+
+
 class EnsembleStepper:
     """Fused GPU time stepping of `nmem` members sharing one basic state."""
 
+    #: precision -> products of the tensor-core Legendre analysis (0: FMA pipes)
+    LEGENDRE = {"fp64": 0, "fp32": 0, "bf16x3": 6, "bf16split": 3}
+
     def __init__(self, sp, vg, bst, damping, semi, vdiff, nmem, precision="fp64",
                  robert=0.04, strictly_linear=False, stream=None):
-        if precision not in ("fp64", "fp32"):
-            raise ValueError("precision must be 'fp64' or 'fp32'")
+        if precision not in self.LEGENDRE:
+            raise ValueError(f"precision must be one of {sorted(self.LEGENDRE)}")
         self.sp, self.vg, self.bst = sp, vg, bst
         self.semi, self.vdiff = semi, vdiff
         self.dev = dev = sp.device
@@ -43,6 +76,7 @@ class EnsembleStepper:
         self.rd = torch.float64 if precision == "fp64" else torch.float32
         self.cd = torch.complex128 if precision == "fp64" else torch.complex64
         self.prec_id = _lib.LBM_F64 if precision == "fp64" else _lib.LBM_F32
+        self.legendre = self.LEGENDRE[precision]
         self.E = E = int(nmem)
         self.N = N = sp.nmax
         self.M = M = N + 1
@@ -113,14 +147,16 @@ class EnsembleStepper:
         self.sf, self.sfs = z(E, M, J, K, 6), z(E, M, J, 5)
         self.af, self.afs = z(E, M, J, K, 7), z(E, M, J, 2)
         self.tend, self.tends = z(E, 4, NS, K), z(E, 2, NS)
+        self.tc_anal = self._tc_anal_image() if self.legendre else None
         # FP32 grid rows between the longitude transforms and the column algebra
-        if precision == "fp32":
+        if precision != "fp64":
             f = lambda *s_: torch.zeros(s_, device=dev, dtype=torch.float32)   # noqa: E731
             self.grid6 = f(E, J, 6 + 6 * K, I)
             self.grid9 = f(E, J, 2 + 9 * K, I)
         else:
             self.grid6 = self.grid9 = None
         self.err = torch.zeros(1, device=dev, dtype=torch.int32)
+        self.err_member = torch.zeros(E, device=dev, dtype=torch.int32)
         self.frc3 = self.frcs = None
         self.frc_shared = 1
         self._dts = []
@@ -128,6 +164,14 @@ class EnsembleStepper:
         self._graphs = {}
         self.pending_ps_mode = 0
         self._desc = None
+        self._oargs = None
+        self._null = torch.empty(0, device=dev, dtype=torch.float32)
+
+    def _tc_anal_image(self):
+        sp = self.sp
+        if self.J % 16:
+            raise ValueError("the tensor-core analysis needs nlat a multiple of 16")
+        return tc_anal_image(sp.pnm, sp.hnm, -sp.laplace, self.N)
 
     # ------------------------------------------------------------------
     def set_timesteps(self, dts):
@@ -223,17 +267,45 @@ class EnsembleStepper:
         self.psb.copy_(psb.reshape(self.E, self.J, self.I))
         self.pending_ps_mode = 0
         self.err.zero_()
+        self.err_member.zero_()
         with torch.cuda.stream(self.stream):
             torch.cuda.current_stream().wait_stream(torch.cuda.default_stream(self.dev))
-            d = self.desc()
-            check(lib().lbm_stepper_colsum(C.byref(d), stream_handle(self.stream)),
-                  "lbm_stepper_colsum")
-            check(lib().lbm_stepper_prime(C.byref(d), stream_handle(self.stream)),
-                  "lbm_stepper_prime")
+            torch.ops.lbm_gb300.stepper_colsum(*self.op_args())
+            torch.ops.lbm_gb300.stepper_prime(*self.op_args())
+
+    def load_zero(self):
+        """Load the zero state (both levels, both grid ps'): the same as
+        load() of zero fields, without transforming them."""
+        with torch.cuda.stream(self.stream):
+            torch.cuda.current_stream().wait_stream(torch.cuda.default_stream(self.dev))
+            for t in (self.sa3, self.sas, self.sb3, self.psa, self.psb, self.err,
+                      self.err_member):
+                t.zero_()
+            self.pending_ps_mode = 0
+            torch.ops.lbm_gb300.stepper_prime(*self.op_args())
+
+    def op_args(self):
+        """(state, work, operators, dims, consts) of the torch.ops.lbm_gb300
+        stepper operators (lists in the orders of ops.STEP_*; an empty tensor
+        stands for NULL)."""
+        if self._desc is not None and self._oargs is not None:
+            return self._oargs
+        z = lambda t: self._null if t is None else t      # noqa: E731
+        state = [getattr(self, n) for n in _ops.STEP_STATE]
+        work = [z(getattr(self, n)) for n in _ops.STEP_WORK]
+        names = {"vdiff": "vdm"}
+        opsl = [z(getattr(self, names.get(n, n))) for n in _ops.STEP_OPS]
+        dims = [self.prec_id, self.E, self.J, self.I, self.N, self.K, len(self._dts),
+                self.strictly_linear] + list(self.vd_on) + [self.frc_shared, self.legendre]
+        consts = [KAPPA, EPSVT, self.robert]
+        self.desc()
+        self._oargs = (state, work, opsl, dims, consts)
+        return self._oargs
 
     def desc(self):
         if self._desc is not None:
             return self._desc
+        self._oargs = None
         d = StepperDesc()
         d.prec = self.prec_id
         d.nmem, d.nlat, d.nlon, d.nmax, d.kmax = self.E, self.J, self.I, self.N, self.K
@@ -253,6 +325,9 @@ class EnsembleStepper:
         d.frcs = ptr(self.frcs)
         d.dft = ptr(self.dft)
         d.err = C.cast(C.c_void_p(self.err.data_ptr()), C.POINTER(C.c_int))
+        d.err_member = C.cast(C.c_void_p(self.err_member.data_ptr()), C.POINTER(C.c_int))
+        d.legendre = self.legendre
+        d.tc_anal = ptr(self.tc_anal)
         self._desc = d
         return d
 
@@ -298,8 +373,9 @@ class EnsembleStepper:
                     check(L.lbm_graph_launch(g, s), "lbm_graph_launch")
                     i += n
                 else:
-                    ctl = self._ctl(planned[i:i + 1])
-                    check(L.lbm_stepper_run(C.byref(d), ctl, 1, s), "lbm_stepper_run")
+                    torch.ops.lbm_gb300.stepper_run(*self.op_args(), [float(dt)],
+                                                    [self.set_index(dt)], [int(psm)],
+                                                    [0 if start else 1])
                     i += 1
         self.pending_ps_mode = pend
 
@@ -327,8 +403,7 @@ class EnsembleStepper:
             return
         self.stream.wait_stream(torch.cuda.default_stream(self.dev))
         with torch.cuda.stream(self.stream):
-            check(lib().lbm_stepper_flush(C.byref(self.desc()), self.pending_ps_mode,
-                                          stream_handle(self.stream)), "lbm_stepper_flush")
+            torch.ops.lbm_gb300.stepper_flush(*self.op_args(), int(self.pending_ps_mode))
         self.pending_ps_mode = 0
 
     # ---- daily history (model.py:257-277) ---------------------------------
@@ -348,12 +423,11 @@ class EnsembleStepper:
         step's kernels) or "ps" (grid ps', after them); mode 0 only records
         the sample (start-up steps), mode 1 adds 0.5 (cur + previous)."""
         names = ("sa3", "sas") if what == "spec" else ("psa",)
-        for name in names:
-            cur = getattr(self, name)
-            prev, acc = self._hist[name]
-            check(lib().lbm_history_accumulate(self.prec_id, acc.numel(), ptr(cur), ptr(prev),
-                                               ptr(acc), 0.5, mode, stream_handle(self.stream)),
-                  "lbm_history_accumulate")
+        with torch.cuda.stream(self.stream):
+            for name in names:
+                cur = getattr(self, name)
+                prev, acc = self._hist[name]
+                torch.ops.lbm_gb300.history_accumulate(cur, prev, acc, 0.5, int(mode))
         if what == "ps" and mode == 1:
             self.hist_n += 1
 
@@ -378,8 +452,20 @@ class EnsembleStepper:
         return spec, ps
 
     def check_finite(self):
+        """False when a member produced a non-finite value (bit 0 of err);
+        raises if a tensor-core kernel gave up a bounded wait (bit 1)."""
         self.stream.synchronize()
-        return int(self.err.item()) == 0
+        e = int(self.err.item())
+        if e & 2:
+            raise RuntimeError("lbm_gb300: a tensor-core kernel timed out waiting for its "
+                               "pipeline (results of this run are invalid)")
+        return (e & 1) == 0
+
+    def bad_members(self):
+        """Indices of the members that produced a non-finite value since the
+        state was loaded (the per-member flags k_implicit sets)."""
+        self.stream.synchronize()
+        return torch.nonzero(self.err_member).flatten().tolist()
 
     def snapshot(self):
         """Copy of the current level (rectangle dict incl. pi)."""

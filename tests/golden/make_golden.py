@@ -3,7 +3,7 @@
 
 Usage (where the reference checkout is available):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the reference checkout>
 
 It imports ``pylbm_isca`` from the given checkout, runs it in FP64 on the
 seeded / analytic inputs of ``lbm_isca_gb300.configs`` and writes small
@@ -216,4 +216,6 @@ def main(refdir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} <path of the reference checkout>")
+    main(sys.argv[1])

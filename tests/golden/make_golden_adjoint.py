@@ -19,7 +19,7 @@ by central differences with eps = 1e-4: D = (F(x0 + eps d) - F(x0 - eps d))
 
 Usage (where the reference checkout is available):
 
-    python tests/golden/make_golden_adjoint.py /root/reference
+    python tests/golden/make_golden_adjoint.py <path of the reference checkout>
 """
 
 import os
@@ -71,4 +71,6 @@ def main(refdir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} <path of the reference checkout>")
+    main(sys.argv[1])

@@ -13,7 +13,7 @@ generated by running the reference package itself:
 
 Usage (where the reference checkout is available):
 
-    python tests/golden/make_golden_io.py /root/reference
+    python tests/golden/make_golden_io.py <path of the reference checkout>
 
 Inputs come from ``bs_inputs.py`` next to this script (seeded, shared with
 the tests).
@@ -112,4 +112,6 @@ def main(refdir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} <path of the reference checkout>")
+    main(sys.argv[1])

@@ -55,6 +55,12 @@ def test_noalloc_stepper_rejects_oversized_cases_without_a_device():
     d.nmem = 0
     assert L.lbm_stepper_run_noalloc(C.byref(d), ctl, 1, None) == _lib.LBM_ERR_ARG
     assert L.lbm_stepper_run_noalloc(None, ctl, 1, None) == _lib.LBM_ERR_ARG
+    # a negative or unsupported longitude count would make the area's size
+    # negative: rejected before the size comparison
+    d.nmem = 1
+    for nlon in (-128, 0, 96):
+        d.nlon = nlon
+        assert L.lbm_stepper_run_noalloc(C.byref(d), ctl, 1, None) == _lib.LBM_ERR_ARG
 
 
 def test_io_and_setup_entry_points_reject_bad_arguments_without_a_device():

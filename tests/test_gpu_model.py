@@ -405,3 +405,38 @@ def test_mjo_forcing_spectral_interpolation_matches_general_loop():
         assert f.counter == 2 * 72 + 2
     for k in ("u", "v", "t", "ps"):
         assert relerr(_np(getattr(out[True], k)), _np(getattr(out[False], k))) < 1e-10, k
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_blowup_names_the_member_and_leaves_the_others_untouched(precision):
+    """A NaN put into one member's heating on the host makes the run raise
+    FloatingPointError (model.py:245-247) naming that member and a window of
+    steps; every other member's state is bitwise that of a clean run."""
+    import torch
+    from lbm_isca_gb300 import Config
+    from lbm_isca_gb300.ensemble import EnsembleForcing, make_ensemble_model
+    sigm = configs.equal_sigma_half_levels(20)
+    bs = configs.solid_body_basic_state(64, 32, sigm)
+    heats, _ = configs.ensemble_heating(64, 32, sigm, 4, seed=3)
+    bad = heats.copy()
+    bad[2, 10, 20, 5] = np.nan
+    states = {}
+    for name, h in (("clean", heats), ("nan", bad)):
+        m, _, _ = make_ensemble_model(
+            bs, 4, Config(ndays=0.5, precision=precision, **configs.plain_damping(20)),
+            device="gb300", nlon=64, nlat=32, nmax=21, sigm=sigm)
+        if name == "nan":
+            with pytest.raises(FloatingPointError, match=r"member 2\b") as ex:
+                m.run(mjo_forcing=EnsembleForcing(h, device="gb300"), verbose=False)
+            assert "between 1 and" in str(ex.value)
+        else:
+            m.run(mjo_forcing=EnsembleForcing(h, device="gb300"), verbose=False)
+        stp = m.stepper()
+        torch.cuda.synchronize()
+        # the spectral levels (the clean run's unload updates only the grid ps')
+        states[name] = (stp.sa3.clone(), stp.sb3.clone(), stp.sas.clone())
+        assert stp.bad_members() == ([2] if name == "nan" else [])
+    for c, n in zip(states["clean"], states["nan"]):
+        assert not torch.isfinite(n[2]).all()
+        for e in (0, 1, 3):
+            assert torch.equal(c[e], n[e]), e

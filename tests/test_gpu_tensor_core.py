@@ -1,0 +1,120 @@
+"""The Legendre analysis on the tensor cores (tcgen05, bfloat16 split
+operands, FP32 accumulation in tensor memory) against an FP64 numpy
+restatement of the same contraction, next to the FP32 FMA kernel it
+replaces; and whole runs in the bf16 modes against the FP64 path."""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import lbm_oracle as orc
+from lbm_isca_gb300 import configs
+
+pytestmark = pytest.mark.gpu
+
+CASES = {"T21L20": (64, 32, 21, 20, 5), "T42L20": (128, 64, 42, 20, 4),
+         "T85L40": (256, 128, 85, 40, 2)}
+
+
+@pytest.fixture(scope="module")
+def torch():
+    t = pytest.importorskip("torch")
+    if not t.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return t
+
+
+def _stepper(torch, case, precision):
+    from lbm_isca_gb300 import Config
+    from lbm_isca_gb300.ensemble import make_ensemble_model
+    nlon, nlat, nmax, K, E = CASES[case]
+    sigm = configs.equal_sigma_half_levels(K)
+    bs = configs.solid_body_basic_state(nlon, nlat, sigm)
+    m, _, _ = make_ensemble_model(bs, E, Config(precision=precision, **configs.plain_damping(K)),
+                                  device="gb300", nlon=nlon, nlat=nlat, nmax=nmax, sigm=sigm)
+    stp = m.stepper()
+    stp.set_timesteps([1200.0])
+    return stp
+
+
+def _oracle_analysis(tr, af, K):
+    """tend [E][4][NS][K] of af [E][M][J][K][7] in FP64: for each m, rows n:
+    vor = i m P.FV + H.FU, div = i m P.FU - H.FV + nn1a P.KE,
+    T = P.T + H.XV, q = P.Q + H.YV (sums over every latitude)."""
+    E, M = af.shape[:2]
+    N = M - 1
+    nn1a = -tr.lap
+    out = []
+    for e in range(E):
+        rows = {f: [] for f in range(4)}
+        for m in range(M):
+            P, H = tr.P[m, m:, :], tr.H[m, m:, :]          # [n][j]
+            x = af[e, m]                                    # [j][k][7]
+            c = lambda T, f: T @ x[:, :, f]                 # noqa: E731  [n][k]
+            rows[0].append(1j * m * c(P, 1) + c(H, 0))
+            rows[1].append(1j * m * c(P, 0) - c(H, 1) + nn1a[m:, None] * c(P, 2))
+            rows[2].append(c(P, 3) + c(H, 4))
+            rows[3].append(c(P, 5) + c(H, 6))
+        out.append(np.stack([np.concatenate(rows[f]) for f in range(4)]))
+    return np.stack(out)
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_analysis_kernel_vs_fp64(torch, case):
+    from lbm_isca_gb300 import _lib
+    from lbm_isca_gb300._lib import StepCtl, check, lib
+    from lbm_isca_gb300.backend import stream_handle
+    nlon, nlat, nmax, K, E = CASES[case]
+    tr = orc.SphericalTransform(nlon, nlat, nmax)
+    rng = np.random.default_rng(17)
+    M, J = nmax + 1, nlat
+    af = (rng.normal(size=(E, M, J, K, 7)) + 1j * rng.normal(size=(E, M, J, K, 7)))
+    afs = (rng.normal(size=(E, M, J, 2)) + 1j * rng.normal(size=(E, M, J, 2)))
+    ref = _oracle_analysis(tr, af, K)
+    got, tends = {}, {}
+    for prec in ("fp32", "bf16x3", "bf16split"):
+        stp = _stepper(torch, case, prec)
+        stp.af.copy_(torch.as_tensor(af, device="cuda").to(torch.complex64))
+        stp.afs.copy_(torch.as_tensor(afs, device="cuda").to(torch.complex64))
+        stp.tend.zero_()
+        ctl = (StepCtl * 1)()
+        ctl[0].dt, ctl[0].set, ctl[0].ps_mode, ctl[0].ra_mode = 1200.0, 0, 0, 1
+        with torch.cuda.stream(stp.stream):
+            check(lib().lbm_stepper_launch(C.byref(stp.desc()), ctl, 1,
+                                           stream_handle(stp.stream)), "analysis")
+        stp.stream.synchronize()
+        assert int(stp.err.item()) == 0
+        got[prec] = stp.tend.cpu().numpy().astype(np.complex128)
+        tends[prec] = stp.tends.cpu().numpy()
+    errs = {p: float(np.linalg.norm(g - ref) / np.linalg.norm(ref)) for p, g in got.items()}
+    # the tensor-core surface part is the FMA kernel's own code
+    assert np.array_equal(tends["bf16x3"], tends["fp32"])
+    assert errs["fp32"] < 2e-6, errs
+    assert errs["bf16x3"] < max(2e-6, 3 * errs["fp32"]), errs
+    assert errs["bf16split"] < 1e-3, errs
+
+
+@pytest.mark.parametrize("precision,tol", [("bf16x3", 1e-5), ("bf16split", 1e-3)])
+def test_bf16_ensemble_against_fp64_at_day10(torch, precision, tol):
+    """Four seeded members at T42L20 for 10 days: every prognostic field
+    within the mode's tolerance of the FP64 path (relative L2 over the packed
+    spectral state)."""
+    from lbm_isca_gb300 import Config
+    from lbm_isca_gb300.ensemble import EnsembleForcing, make_ensemble_model
+    sigm = configs.equal_sigma_half_levels(20)
+    bs = configs.solid_body_basic_state(128, 64, sigm)
+    heats, _ = configs.ensemble_heating(128, 64, sigm, 4, seed=1)
+    out = {}
+    for prec in ("fp64", precision):
+        m, _, _ = make_ensemble_model(
+            bs, 4, Config(ndays=10.0, precision=prec, **configs.plain_damping(20)),
+            device="gb300", nlon=128, nlat=64, nmax=42, sigm=sigm)
+        m.run(mjo_forcing=EnsembleForcing(heats, device="gb300"), verbose=False)
+        a, _ = m.stepper().spectral_state()
+        out[prec] = {k: v.cpu() for k, v in a.items()}
+    for k in ("vor", "div", "t", "pi"):
+        r, f = out["fp64"][k], out[precision][k]
+        e = float(torch.linalg.norm(f - r) / torch.linalg.norm(r))
+        assert e <= tol, (k, e)
+    assert float(out[precision]["q"].abs().max()) == 0.0

@@ -174,3 +174,38 @@ def test_mjo_forcing_call_sequence_and_plan():
     assert vals[2:6] == [1.0, 1.25, 1.5, 1.75]
     assert vals[6:10] == [2.0, 2.25, 2.5, 2.75]
     assert vals[10:12] == [3.0, 3.0]
+
+
+def test_tensor_core_table_image_layout():
+    """The tc_anal table image: every element sits at the byte the header
+    gives, (m, s) blocks in order, three tables x three bfloat16 pieces per
+    block, and the pieces sum to the FP64 table to 2^-24 (checked on the CPU
+    against the oracle's tables)."""
+    import torch
+    from oracle import lbm_oracle as orc
+    from lbm_isca_gb300.stepper import tc_anal_image
+    N, J = 21, 32
+    tr = orc.SphericalTransform(64, 32, N)
+    P, H = torch.as_tensor(tr.P), torch.as_tensor(tr.H)
+    nn1a = torch.as_tensor(-tr.lap)
+    img = tc_anal_image(P, H, nn1a, N).numpy().view(np.uint16)
+    tabs = (tr.P, tr.H, tr.P * (-tr.lap)[None, :, None])
+    KS = J // 16
+
+    def bf16(u):      # bfloat16 bits -> float
+        return (u.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+    base = 0
+    rng = np.random.default_rng(0)
+    for m in range(N + 1):
+        nr = N + 1 - m
+        nb = (nr + 15) // 16 * 16
+        for _ in range(40):
+            s, t = rng.integers(KS), rng.integers(3)
+            r, kk = rng.integers(nb), rng.integers(16)
+            tile = base + s * 9 * nb * 16
+            off = (r // 8) * 128 + (kk // 8) * 64 + (r % 8) * 8 + kk % 8
+            val = sum(bf16(img[tile + (t * 3 + p) * nb * 16 + off]) for p in range(3))
+            ref = tabs[t][m, m + r, s * 16 + kk] if r < nr else 0.0
+            assert abs(val - ref) <= 2.0 ** -24 * abs(ref) + 1e-300, (m, s, t, r, kk)
+        base += KS * 9 * nb * 16
+    assert base == img.size
