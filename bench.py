@@ -230,6 +230,34 @@ def build_model(E, precision, torch, days=1.0, seed=SEED, device="cuda"):
     return model, heats
 
 
+def step_roofline(E, p, ms_per_step, peaks, precision):
+    """The whole step against its lower bound, with the per-member-step counts
+    of the reference algorithm: Legendre flops 4 NS J (33 K + 6), DFT flops
+    (21 K + 6) J 2.5 I log2 I, unavoidable HBM bytes = the state read and
+    written (4 (4 K + 1) NS 2 p) plus the grid forcing (K J I p).  T_min =
+    transform flops / contraction peak + unavoidable bytes / HBM peak; the
+    contraction peak is the measured bf16 tensor rate for the tensor-core
+    modes and the FP32 FMA rate (152 SMs x 128 lanes x 2 x max clock) for the
+    FMA path."""
+    nlon, nlat, nmax = GRID
+    J, I, K = nlat, nlon, K_LEV
+    NS = (nmax + 1) * (nmax + 2) // 2
+    leg = 4.0 * NS * J * (33 * K + 6)
+    dft = (21 * K + 6) * J * 2.5 * I * math.log2(I)
+    byt = 4.0 * (4 * K + 1) * NS * 2 * p + K * J * I * p
+    hbm = float(peaks.get("hbm_gbs", 6800.0)) * 1e9
+    if precision in ("bf16x3", "bf16split"):
+        pk, pk_name = float(peaks.get("bf16_tflops", 1900.0)) * 1e12, "bf16 tensor (measured)"
+    else:
+        mhz = float(peaks.get("sm_max_mhz", 2070.0))
+        pk, pk_name = 152 * 128 * 2 * mhz * 1e6, "FP32 FMA (152 SMs x 128 x 2 x max clock)"
+    t_min = E * (leg + dft) / pk + E * byt / hbm
+    return {"t_min_ms": 1e3 * t_min, "t_measured_ms": ms_per_step,
+            "frac": 1e3 * t_min / ms_per_step,
+            "per_member_step": {"legendre_flop": leg, "dft_flop": dft, "unavoidable_bytes": byt},
+            "contraction_peak": pk_name}
+
+
 def algorithmic_bytes(E, p):
     """HBM bytes each stepper kernel must move per launch (p = bytes/real):
     every array it reads or writes once, per-member arrays times E, the shared
@@ -676,6 +704,7 @@ def main():
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": read_traffic(names[top], E),
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+            "roofline_step": step_roofline(E, p, t_max / args.steps, peaks, args.precision),
             "kernel_ms": dict(zip(names, [float(x) for x in kern_ms])),
             "kernel_share": dict(zip(names, [float(x / kern_ms.sum()) for x in kern_ms])),
             "algorithmic_gbs": {n: ab[n] / (kern_ms[i] / 1000.0) / 1e9
@@ -716,11 +745,13 @@ def end_to_end(args, E, heats, torch):
         m2.cfg.phase_timing = profile
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        dev_heat = host_heat.to("cuda", non_blocking=True)
+        # H2D and D2H over the CPU-GPU link (SM loads / stores of pinned memory)
+        dev_heat = torch.empty(tuple(host_heat.shape), device="cuda", dtype=host_heat.dtype)
+        torch.ops.lbm_gb300.link_copy_(dev_heat, host_heat)
         m2.run(mjo_forcing=EnsembleForcing(dev_heat, device="cuda"), verbose=False)
         t1 = time.perf_counter()
         for k in fields:
-            host_out[k].copy_(getattr(m2.ga, k), non_blocking=True)
+            torch.ops.lbm_gb300.link_copy_(host_out[k], getattr(m2.ga, k).contiguous())
         torch.cuda.synchronize()
         t2 = time.perf_counter()
         return t2 - t0, t2 - t1
@@ -740,7 +771,8 @@ def end_to_end(args, E, heats, torch):
             "phases_s": phases,
             "note": "LBM.run of the ensemble from pinned host heatings (H2D inside), "
                     f"{args.steps} advancing + 2 start-up steps, final grid state copied "
-                    "to pinned host buffers (D2H inside); after one untimed run; "
+                    "to pinned host buffers (D2H inside); both copies by lbm_link_copy "
+                    "(SM loads/stores over NVLink-C2C); after one untimed run; "
                     "phases_s from a further run synchronised at phase boundaries"}
 
 

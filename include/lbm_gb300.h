@@ -257,11 +257,12 @@ int lbm_implicit_step_adjoint(int prec, const lbm_implicit_adj_args* a, void* st
  *        members that blew up (the reference's FloatingPointError,
  *        model.py:245-247); the kernels only ever set these flags, the caller
  *        clears them
- *   legendre: 0 = the Legendre analysis on the FP32 FMA pipes; 3 or 6 = on
- *        the tensor cores (tcgen05, FP32 mode only): af split into three
- *        bfloat16 pieces, products summed in FP32 in tensor memory, 6 = the
- *        six products down to third order (FP32-level accuracy), 3 = the
- *        three products of a two-way split (about 16 bits)
+ *   legendre: 0 = the Legendre analysis and synthesis on the FP32 FMA
+ *        pipes; 3 or 6 = their level fields on the tensor cores (tcgen05,
+ *        FP32 mode only): operands split into three bfloat16 pieces,
+ *        products summed in FP32 in tensor memory, 6 = the six products down
+ *        to third order (FP32-level accuracy), 3 = the three products of a
+ *        two-way split (about 16 bits)
  *   tc_anal: table image of the tensor-core analysis (legendre != 0), 16-byte
  *        aligned: for m = 0..N, for each step s of 16 latitudes, the tables
  *        P, H and nn1a P (in that order), each as three bfloat16 pieces
@@ -270,6 +271,14 @@ int lbm_implicit_step_adjoint(int prec, const lbm_implicit_adj_args* a, void* st
  *        16; rows n - m, zero past N) whose element (r, kk) sits at byte
  *        (r / 8) 256 + (kk / 8) 128 + (r % 8) 16 + (kk % 8) 2; needs nlat a
  *        multiple of 16 and kmax even
+ *   tc_synth: table image of the tensor-core synthesis (legendre != 0),
+ *        16-byte aligned: JT = nlat if 6 nlat <= 512 latitudes fit, else
+ *        nlat / 2 (two parts); for m = 0..N, for each part, for each step s
+ *        of 16 rows n = m + 16 s + kk, the tables m P il, -H il, H il and P
+ *        (il = -a^2 / (n (n + 1)), the inverse Laplacian factor of row
+ *        n (zero for n = 0; rows past N are zero), each as three bfloat16
+ *        pieces, each piece a JT x 16 tile (rows = latitudes of the part,
+ *        K = kk) in the layout of tc_anal
  * sf, af and grid9 must be 16-byte aligned (LBM_ERR_ARG otherwise).
  * ==========================================================================*/
 enum {
@@ -293,6 +302,7 @@ typedef struct lbm_stepper_desc {
   int* err_member;
   int legendre;
   const void* tc_anal;
+  const void* tc_synth;
 } lbm_stepper_desc;
 
 /* Per-step control.  dt: time step of this call; set: which operator set
@@ -383,6 +393,17 @@ int lbm_z2ps(int64_t ncol, int nk, const double* z, const double* zs, const doub
 int lbm_spline(int64_t ncol, int nk, int nl, const double* x, const double* z, const double* xi,
                double* out, int omisb, int omist, double xmiss, void* stream);
 int lbm_zonal_filter(int nlat, int nlon, int nk, double* x, int mode, void* stream);
+
+/* ---- Host <-> device transfers over the CPU-GPU link -------------------------
+ * No counterpart in the reference (its arrays move by cupy.asarray /
+ * cupy.asnumpy, backend.py:80-105).  Copies `bytes` from src to dst with SM
+ * loads and stores, so that on a node whose CPU and GPU share a coherent
+ * link (NVLink-C2C on Grace-Blackwell) pinned host memory is read or written
+ * at the link's rate rather than a copy engine's.  Each pointer is device
+ * memory or pinned host memory that the device can address (cudaHostAlloc /
+ * cudaHostRegister; pageable memory gives LBM_ERR_ARG); both 16-byte aligned;
+ * any byte count.  Asynchronous on `stream`, like cudaMemcpyAsync. */
+int lbm_link_copy(void* dst, const void* src, int64_t bytes, void* stream);
 
 /* ---- Stepping without allocating -------------------------------------------
  * No counterpart in the reference, whose step functions allocate their work

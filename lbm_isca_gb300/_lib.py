@@ -78,7 +78,7 @@ class StepperDesc(C.Structure):
                                      "sb3", "psa", "psb", "sf", "sfs", "af", "afs", "tend",
                                      "tends", "grid6", "grid9")]
                 + [("err", C.POINTER(I32)), ("err_member", C.POINTER(I32)),
-                   ("legendre", I32), ("tc_anal", VP)])
+                   ("legendre", I32), ("tc_anal", VP), ("tc_synth", VP)])
 
 
 class StepCtl(C.Structure):
@@ -113,6 +113,7 @@ _SIGS = {
     "lbm_graph_destroy": (I32, [VP]),
     "lbm_stepper_run_noalloc": (I32, [C.POINTER(StepperDesc), C.POINTER(StepCtl), I32, VP]),
     "lbm_history_accumulate": (I32, [I32, C.c_int64, VP, VP, VP, F64, I32, VP]),
+    "lbm_link_copy": (I32, [VP, VP, C.c_int64, VP]),
     "lbm_grads_records": (I32, [C.c_int64, I32, C.POINTER(VP), I32, F64, F64, VP, VP]),
     "lbm_z2ps": (I32, [C.c_int64, I32, VP, VP, VP, VP, VP]),
     "lbm_spline": (I32, [C.c_int64, I32, I32, VP, VP, VP, VP, I32, I32, F64, VP]),

@@ -26,22 +26,25 @@
 //                 contiguous run per member) and its table image, into a
 //                 two-stage ring;
 //   warp 1        TMEM allocation and the MMA issue (one thread);
-//   warps 2..9    conversion: staged FP32 af -> the nine split A tiles, four
-//                 A slots in a ring;
-//   warps 10..13  epilogue: tcgen05.ld of the four regions -> tend.
+//   warps 2..17   conversion: staged FP32 af -> the nine split A tiles, six
+//                 A slots in a ring; warps 2..9 take the even tiles, 10..17
+//                 the odd ones;
+//   warps 18..21  epilogue: tcgen05.ld of the four regions -> tend.
 // Every wait is bounded (tc::mbar_wait); a timeout sets bit 2 of *err and
 // the CTA winds down without leaving copies or MMAs in flight.
 #pragma once
 #include "tc_common.cuh"
+#include "async_copy.cuh"
 
 namespace lbm {
 
 constexpr int ATC_STAGES = 2;
-constexpr int ATC_ASLOTS = 4;
-constexpr int ATC_CONV_WARPS = 8;
+constexpr int ATC_ASLOTS = 6;
+constexpr int ATC_CONV_WARPS = 16;     // two groups of 8: even / odd A matrices
 constexpr int ATC_THREADS = 32 * (2 + ATC_CONV_WARPS + 4);
 constexpr int ATC_NMAT = 9;
 constexpr int ATC_ERR = 2;            // *err bit set by a timed-out wait
+constexpr unsigned ATC_PREFETCH = 6;  // steps of af rows pulled into L2 ahead
 
 LBM_HD int atc_nb(int N, int m) { return ((N + 1 - m) + 15) / 16 * 16; }
 
@@ -85,36 +88,94 @@ struct AtcSmem {
   unsigned tslot;
 };
 
-// A matrix am -> (table, region): tables 0 = P, 1 = H, 2 = nn1a P; regions
-// 0 = vor, 1 = div, 2 = T, 3 = q.
-__constant__ int c_atc_tab[ATC_NMAT] = {0, 1, 0, 1, 2, 0, 1, 0, 1};
-__constant__ int c_atc_reg[ATC_NMAT] = {0, 0, 1, 1, 1, 2, 2, 3, 3};
-// split pieces (A, table) of the six products, smallest first; the last three
-// are the two-way (three-product) form
-__constant__ int c_atc_pa[6] = {2, 1, 0, 1, 0, 0};
-__constant__ int c_atc_pb[6] = {0, 1, 2, 0, 1, 0};
+// A matrix am = 0..8: (i m FV) P, FU H -> vor; (i m FU) P, (-FV) H, KE (nn1a P)
+// -> div; T P, XV H -> T; Q P, YV H -> q.  Tables 0 = P, 1 = H, 2 = nn1a P;
+// regions 0 = vor, 1 = div, 2 = T, 3 = q.  The split pieces (A, table) of
+// the six products, smallest first, are (2,0) (1,1) (0,2) (1,0) (0,1)
+// (0,0); the last three are the two-way (three-product) form.
 
-// Value of A matrix am for Re (ri = 0) or Im (ri = 1) of one level, from the
-// staged af row c (7 complex fields of one (member, latitude, level)).
-LBM_D float atc_value(int am, const float* c, int ri, float rm) {
+// A matrix AM -> (table, region) at compile time (the same as the tables above).
+template <int AM> struct AtcMat {
+  static constexpr int tab = AM == 1 || AM == 3 || AM == 6 || AM == 8 ? 1 : AM == 4 ? 2 : 0;
+  static constexpr int reg = AM < 2 ? 0 : AM < 5 ? 1 : AM < 7 ? 2 : 3;
+  static constexpr int field = AM == 0 || AM == 3 ? AF_FV : AM == 1 || AM == 2 ? AF_FU
+                             : AM == 4 ? AF_KE : AM == 5 ? AF_T : AM == 6 ? AF_XV
+                             : AM == 7 ? AF_Q : AF_YV;
+  static constexpr bool swap = AM == 0 || AM == 2;     // times i m: Re and Im swap
+  static constexpr bool neg = AM == 3;
+};
+
+// One thread's part of A tile AM: the 8 latitudes of chunk ch of row
+// (member, level, ri), read from the staged af rows (stride jst floats) and
+// split into the tile's three pieces.
+template <int AM>
+LBM_D void atc_convert(const float* rows, size_t jst, int ri, float rm, unsigned char* at,
+                       unsigned off) {
+  using T = AtcMat<AM>;
+  const int c = 2 * T::field + (T::swap ? 1 - ri : ri);
+  const float sc = T::swap ? (ri ? rm : -rm) : (T::neg ? -1.0f : 1.0f);
+  float x[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) x[q] = (T::swap || T::neg) ? sc * rows[q * jst + c]
+                                                          : rows[q * jst + c];
+  tc::split3_store8(x, at + off, at + 4096 + off, at + 8192 + off);
+}
+LBM_D void atc_convert_any(int am, const float* rows, size_t jst, int ri, float rm,
+                           unsigned char* at, unsigned off) {
   switch (am) {
-    case 0: return ri ? rm * c[2 * AF_FV] : -rm * c[2 * AF_FV + 1];     // (i m FV)
-    case 1: return c[2 * AF_FU + ri];
-    case 2: return ri ? rm * c[2 * AF_FU] : -rm * c[2 * AF_FU + 1];     // (i m FU)
-    case 3: return -c[2 * AF_FV + ri];
-    case 4: return c[2 * AF_KE + ri];
-    case 5: return c[2 * AF_T + ri];
-    case 6: return c[2 * AF_XV + ri];
-    case 7: return c[2 * AF_Q + ri];
-    default: return c[2 * AF_YV + ri];
+    case 0: atc_convert<0>(rows, jst, ri, rm, at, off); break;
+    case 1: atc_convert<1>(rows, jst, ri, rm, at, off); break;
+    case 2: atc_convert<2>(rows, jst, ri, rm, at, off); break;
+    case 3: atc_convert<3>(rows, jst, ri, rm, at, off); break;
+    case 4: atc_convert<4>(rows, jst, ri, rm, at, off); break;
+    case 5: atc_convert<5>(rows, jst, ri, rm, at, off); break;
+    case 6: atc_convert<6>(rows, jst, ri, rm, at, off); break;
+    case 7: atc_convert<7>(rows, jst, ri, rm, at, off); break;
+    default: atc_convert<8>(rows, jst, ri, rm, at, off); break;
+  }
+}
+
+// The MMAs of one A tile AM: the split products (smallest first, from q0)
+// into its region; `initm` marks the regions already written in this unit.
+template <int AM>
+LBM_D void atc_issue(unsigned dbase, int NB, uint64_t adesc, uint64_t bdesc0, unsigned tstride,
+                     unsigned idesc, int q0, unsigned& initm) {
+  using T = AtcMat<AM>;
+  const unsigned dcol = dbase + (unsigned)(T::reg * NB);
+  // descriptor address fields advance by (bytes >> 4)
+  const uint64_t bt = bdesc0 + (uint64_t)((T::tab * 3 * tstride) >> 4);
+  bool acc = (initm >> T::reg) & 1u;
+  const int pa[6] = {2, 1, 0, 1, 0, 0}, pb[6] = {0, 1, 2, 0, 1, 0};
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    if (q < q0) continue;
+    tc::mma_bf16(dcol, adesc + (uint64_t)((pa[q] * 4096u) >> 4),
+             bt + (uint64_t)((pb[q] * tstride) >> 4), idesc, acc);
+    acc = true;
+  }
+  initm |= 1u << T::reg;
+}
+LBM_D void atc_issue_any(int am, unsigned dbase, int NB, uint64_t adesc, uint64_t bdesc0,
+                         unsigned tstride, unsigned idesc, int q0, unsigned& initm) {
+  switch (am) {
+    case 0: atc_issue<0>(dbase, NB, adesc, bdesc0, tstride, idesc, q0, initm); break;
+    case 1: atc_issue<1>(dbase, NB, adesc, bdesc0, tstride, idesc, q0, initm); break;
+    case 2: atc_issue<2>(dbase, NB, adesc, bdesc0, tstride, idesc, q0, initm); break;
+    case 3: atc_issue<3>(dbase, NB, adesc, bdesc0, tstride, idesc, q0, initm); break;
+    case 4: atc_issue<4>(dbase, NB, adesc, bdesc0, tstride, idesc, q0, initm); break;
+    case 5: atc_issue<5>(dbase, NB, adesc, bdesc0, tstride, idesc, q0, initm); break;
+    case 6: atc_issue<6>(dbase, NB, adesc, bdesc0, tstride, idesc, q0, initm); break;
+    case 7: atc_issue<7>(dbase, NB, adesc, bdesc0, tstride, idesc, q0, initm); break;
+    default: atc_issue<8>(dbase, NB, adesc, bdesc0, tstride, idesc, q0, initm); break;
   }
 }
 
 __global__ void __launch_bounds__(ATC_THREADS, 1)
     k_anal_tc(SD<float> d, const unsigned char* __restrict__ tabs, AtcPlan pl, int nprod) {
   extern __shared__ unsigned char smraw_tc[];
-  unsigned char* base = reinterpret_cast<unsigned char*>(
-      (reinterpret_cast<uintptr_t>(smraw_tc) + 1023) & ~uintptr_t(1023));
+  // 1 KB alignment by pointer arithmetic on the shared array itself, so
+  // that every access below stays a shared-memory access (not generic)
+  unsigned char* base = smraw_tc + ((1024u - (tc::smem_addr(smraw_tc) & 1023u)) & 1023u);
   AtcSmem* sm = reinterpret_cast<AtcSmem*>(base);
   unsigned char* stages = base + 1024;
   unsigned char* aring = stages + ATC_STAGES * pl.stage_bytes;
@@ -129,7 +190,7 @@ __global__ void __launch_bounds__(ATC_THREADS, 1)
       mbar_init(smem_addr(&sm->empty[i]), 1);
     }
     for (int i = 0; i < ATC_ASLOTS; ++i) {
-      mbar_init(smem_addr(&sm->afull[i]), ATC_CONV_WARPS);
+      mbar_init(smem_addr(&sm->afull[i]), ATC_CONV_WARPS / 2);
       mbar_init(smem_addr(&sm->aempty[i]), 1);
     }
     for (int i = 0; i < 2; ++i) {
@@ -154,14 +215,28 @@ __global__ void __launch_bounds__(ATC_THREADS, 1)
     // ---------------- producer ----------------
     if (lane == 0) {
       unsigned t = 0;
+      const unsigned rowb = (unsigned)(16 * K * 7 * 8);
+      // the af rows of step t (the t-th step of this CTA's units) pulled into
+      // L2 ahead of their bulk copy, ATC_PREFETCH steps early
+      auto prefetch = [&](unsigned tp) {
+        const int u = blockIdx.x + (int)(tp / KS) * gridDim.x, s = (int)(tp % KS);
+        if (u >= pl.nunits) return;
+        const int m = u / pl.ngroups, g = u - m * pl.ngroups;
+        const int e0 = g * pl.G, gm = min(pl.G, E - e0);
+        for (int mi = 0; mi < gm; ++mi)
+          prefetch_l2_bulk(reinterpret_cast<const float*>(d.af) +
+                               ((((size_t)(e0 + mi) * M + m) * J + s * 16) * K) * 14,
+                           rowb);
+      };
+      for (unsigned tp = 0; tp < ATC_PREFETCH; ++tp) prefetch(tp);
       for (int u = blockIdx.x; u < pl.nunits && ok; u += gridDim.x) {
         const int m = u / pl.ngroups, g = u - m * pl.ngroups;
         const int e0 = g * pl.G, gm = min(pl.G, E - e0);
         const int nb = atc_nb(N, m);
         const unsigned tb = 9u * nb * 32u;
-        const unsigned rowb = (unsigned)(16 * K * 7 * 8);
         const unsigned char* tm = tabs + atc_tab_offset(N, KS, m);
         for (int s = 0; s < KS && ok; ++s, ++t) {
+          prefetch(t + ATC_PREFETCH);
           const int st = t % ATC_STAGES;
           const unsigned ph = (t / ATC_STAGES) & 1u;
           ok = mbar_wait(smem_addr(&sm->empty[st]), ph ^ 1u, err, ATC_ERR);
@@ -199,27 +274,21 @@ __global__ void __launch_bounds__(ATC_THREADS, 1)
         if (!ok) break;
         tc_fence_after();
         const unsigned dbase = tbase + (unsigned)(b * 4 * NB);
-        bool init[4] = {false, false, false, false};
+        unsigned initm = 0;
+        const unsigned tstride = (unsigned)nb * 32u;
         for (int s = 0; s < KS && ok; ++s, ++t) {
           const int st = t % ATC_STAGES;
           ok = mbar_wait(smem_addr(&sm->full[st]), (t / ATC_STAGES) & 1u, err, ATC_ERR);
           if (!ok) break;
           const unsigned char* sd = stages + st * pl.stage_bytes;
-          const unsigned stab = smem_addr(sd + (pl.data_bytes + 1023) / 1024 * 1024);
+          const uint64_t bdesc0 = smem_desc(smem_addr(sd + (pl.data_bytes + 1023) / 1024 * 1024));
           for (int am = 0; am < ATC_NMAT; ++am, ++a) {
             const int slot = a % ATC_ASLOTS;
             ok = mbar_wait(smem_addr(&sm->afull[slot]), (a / ATC_ASLOTS) & 1u, err, ATC_ERR);
             if (!ok) break;
             tc_fence_after();
-            const int reg = c_atc_reg[am], tab = c_atc_tab[am];
-            const unsigned dcol = dbase + (unsigned)(reg * NB);
-            const unsigned abase = smem_addr(aring + slot * pl.a_bytes);
-            for (int q = q0; q < 6; ++q) {
-              const uint64_t ad = smem_desc(abase + c_atc_pa[q] * 4096u);
-              const uint64_t bd = smem_desc(stab + (unsigned)((tab * 3 + c_atc_pb[q]) * nb * 32));
-              mma_bf16(dcol, ad, bd, idesc, init[reg]);
-              init[reg] = true;
-            }
+            atc_issue_any(am, dbase, NB, smem_desc(smem_addr(aring + slot * pl.a_bytes)), bdesc0,
+                          tstride, idesc, q0, initm);
             mma_commit(smem_addr(&sm->aempty[slot]));
           }
           if (!ok) break;
@@ -235,7 +304,8 @@ __global__ void __launch_bounds__(ATC_THREADS, 1)
   } else if (warp < 2 + ATC_CONV_WARPS) {
     // ---------------- conversion ----------------
     const int ct = threadIdx.x - 64;
-    const int row = ct & 127, ch = ct >> 7;       // A row, 8-latitude chunk
+    const int grp = ct >> 8;                      // 0: even A matrices, 1: odd
+    const int row = ct & 127, ch = (ct >> 7) & 1;   // A row, 8-latitude chunk
     const int twoK = 2 * K;
     const int mi = row / twoK, rem = row - mi * twoK, k = rem >> 1, ri = rem & 1;
     unsigned t = 0, a = 0;
@@ -252,23 +322,20 @@ __global__ void __launch_bounds__(ATC_THREADS, 1)
         // the 8 staged rows of this thread's chunk: (member mi, latitude, level k)
         const float* rows = sd + ((size_t)(mi * 16 + ch * 8) * K + k) * 14;
         const size_t jst = (size_t)K * 14;
-        for (int am = 0; am < ATC_NMAT; ++am, ++a) {
-          const int slot = a % ATC_ASLOTS;
-          ok = warp_wait(smem_addr(&sm->aempty[slot]), ((a / ATC_ASLOTS) & 1u) ^ 1u, err,
+        for (int am = grp; am < ATC_NMAT; am += 2) {
+          const unsigned aa = a + (unsigned)am;      // this tile's place in the A ring
+          const int slot = aa % ATC_ASLOTS;
+          ok = warp_wait(smem_addr(&sm->aempty[slot]), ((aa / ATC_ASLOTS) & 1u) ^ 1u, err,
                          ATC_ERR);
           if (!ok) break;
-          unsigned char* at = aring + slot * pl.a_bytes;
-          if (live) {
-            float x[8];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) x[q] = atc_value(am, rows + q * jst, ri, rm);
-            const unsigned off = tile_offset(row, ch * 8);
-            split3_store8(x, at + off, at + 4096 + off, at + 8192 + off);
-          }
+          if (live)
+            atc_convert_any(am, rows, jst, ri, rm, aring + slot * pl.a_bytes,
+                            tile_offset(row, ch * 8));
           fence_async_smem();
           __syncwarp();
           if (lane == 0) mbar_arrive(smem_addr(&sm->afull[slot]));
         }
+        a += ATC_NMAT;
       }
     }
   } else {

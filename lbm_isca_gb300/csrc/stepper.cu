@@ -52,6 +52,7 @@ template <typename R> struct SD {
   int* err_member;
   int legendre;                          // 0 FMA; 3 or 6: tensor-core products
   const unsigned char* tc_anal;          // table image of k_anal_tc
+  const unsigned char* tc_synth;         // table image of k_synth_tc
 };
 
 template <typename R> SD<R> make_sd(const lbm_stepper_desc& d) {
@@ -79,6 +80,7 @@ template <typename R> SD<R> make_sd(const lbm_stepper_desc& d) {
   s.err_member = d.err_member;
   s.legendre = d.legendre;
   s.tc_anal = (const unsigned char*)d.tc_anal;
+  s.tc_synth = (const unsigned char*)d.tc_synth;
   return s;
 }
 
@@ -372,6 +374,9 @@ template <typename R> struct PairRows {
 // two partial groups).
 template <int NC> LBM_HD int anal_groups(int N) { return (N + 2 + NC - 1) / NC + 1; }
 
+// Members per block of the surface-only forms (one table staging serves them).
+constexpr int SURF_EB = 16;
+
 // SURF: only the surface part (tends), for the tensor-core analysis, which
 // computes the level part (k_anal_tc).
 template <typename R, int NC, int KC, bool SURF = false>
@@ -517,8 +522,9 @@ __global__ void k_anal(SD<R> d) {
     }
   }
   }  // !SURF
-  // surface: wt_pi and pi(t - dt), one thread per row (first level chunk only)
-  if (kc != 0) return;
+  // surface: wt_pi and pi(t - dt), one thread per row (first level chunk
+  // only; the surface-only form takes SURF_EB members per block)
+  auto surface = [&](int e) {
   __syncthreads();
   C2<R>* ss = raw;                                   // [2][JH][2 fields][2]
   for (int idx = tid; idx < nm * JH * 2; idx += nt) {
@@ -546,6 +552,14 @@ __global__ void k_anal(SD<R> d) {
     const size_t idx = (size_t)spec_index(m, n, N);
     d.tends[((size_t)e * 2 + 0) * d.NS + idx] = a0;
     d.tends[((size_t)e * 2 + 1) * d.NS + idx] = a1;
+  }
+  };
+  if constexpr (SURF) {
+    const int e1 = min(d.E, (int)(blockIdx.y + 1) * SURF_EB);
+    for (int ee = blockIdx.y * SURF_EB; ee < e1; ++ee) surface(ee);
+  } else {
+    if (kc != 0) return;
+    surface(e);
   }
 }
 
@@ -786,7 +800,9 @@ LBM_D void store_pair(C2<double>* o, C2<double> a, C2<double> b) {
 // =============================================================================
 constexpr int SY_THREADS = 320;
 
-template <typename R, int JG, int KC, int HV>
+// SURF: only the surface fields (sfs), for the tensor-core synthesis, which
+// computes the level fields (k_synth_tc).
+template <typename R, int JG, int KC, int HV, bool SURF = false>
 __global__ void __launch_bounds__(SY_THREADS, 2) k_synth(SD<R> d) {
   const int p = blockIdx.x, e = blockIdx.y, kc = blockIdx.z;
   const int J = d.J, K = d.K, N = d.N, M = d.M, JH = J / 2, NS = d.NS;
@@ -804,6 +820,8 @@ __global__ void __launch_bounds__(SY_THREADS, 2) k_synth(SD<R> d) {
     tp[idx] = d.symp[(size_t)row * JH + jh];
     th[idx] = d.symh[(size_t)row * JH + jh];
   }
+  const int nm = pr.L2 ? 2 : 1;
+  if constexpr (!SURF) {
   const size_t e3 = (size_t)e * 4 * NS * K;
   for (int idx = tid; idx < pr.NR * kn; idx += nt) {
     const int r = idx / kn, kk = idx % kn;
@@ -824,7 +842,6 @@ __global__ void __launch_bounds__(SY_THREADS, 2) k_synth(SD<R> d) {
   const int NJG = (JH + JG - 1) / JG;
   const size_t jmK = (size_t)J * K;
   C2<R>* sfe = d.sf + (size_t)e * M * jmK * SF_N;
-  const int nm = pr.L2 ? 2 : 1;
   // Items: (term half, latitude group, level), level fastest.  With HV = 2
   // the first NJG KC items take the wind terms (P chi, H psi, P psi, H chi ->
   // U, V), the rest the scalar terms (P vor, P div, P T, P q): each value read
@@ -927,8 +944,11 @@ __global__ void __launch_bounds__(SY_THREADS, 2) k_synth(SD<R> d) {
     if (half != 0) scalars();
    }
   }
-  // surface fields (first level chunk only)
-  if (kc != 0) return;
+  }  // !SURF
+  // surface fields (first level chunk only; the surface-only form takes
+  // SURF_EB members per block)
+  if constexpr (SURF) __syncthreads();
+  auto surface = [&](int e) {
   const size_t es = (size_t)e * 4 * NS;
   for (int it = tid; it < nm * JH; it += nt) {
     const int jh = it % JH, mm = it / JH;
@@ -970,6 +990,14 @@ __global__ void __launch_bounds__(SY_THREADS, 2) k_synth(SD<R> d) {
       o[SFS_DH] = comb(6);
     }
   }
+  };
+  if constexpr (SURF) {
+    const int e1 = min(d.E, (int)(blockIdx.y + 1) * SURF_EB);
+    for (int ee = blockIdx.y * SURF_EB; ee < e1; ++ee) surface(ee);
+  } else {
+    if (kc != 0) return;
+    surface(e);
+  }
 }
 
 // Apply the pending grid-ps update at the end of a run (see k_grid).
@@ -1006,6 +1034,7 @@ __global__ void k_ps_flush(SD<R> d, int ps_mode) {
 }  // namespace lbm
 #include "grid_split.cuh"
 #include "legendre_tc.cuh"
+#include "synth_tc.cuh"
 namespace lbm {
 
 // ---- launch configuration ------------------------------------------------------
@@ -1049,7 +1078,7 @@ template <typename R, int KC> void launch_anal(const SD<R>& d, cudaStream_t st, 
     cudaFuncSetAttribute(k_anal<R, NC, KC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)sm);
   } else if (d.legendre && sizeof(R) == 4) {
-    k_anal<R, NC, KC, true><<<dim3(NP, d.E, 1), nt, sm, st>>>(d);
+    k_anal<R, NC, KC, true><<<dim3(NP, (d.E + SURF_EB - 1) / SURF_EB, 1), nt, sm, st>>>(d);
   } else {
     k_anal<R, NC, KC><<<dim3(NP, d.E, (d.K + KC - 1) / KC), nt, sm, st>>>(d);
   }
@@ -1058,6 +1087,7 @@ template <typename R> void run_anal(const SD<R>& d, cudaStream_t st, bool attrs)
   if (anal_kc<R>(d.N) == Cfg<R>::KCA) launch_anal<R, Cfg<R>::KCA>(d, st, attrs);
   else launch_anal<R, Cfg<R>::KCA / 2>(d, st, attrs);
 }
+inline int persistent_grid(const void* fn, int nt, size_t smem, int units);
 template <typename R> size_t synth_smem(int NR, int JH) {
   return sizeof(R) * 2 * (size_t)NR * JH + sizeof(C2<R>) * (size_t)NR * Cfg<R>::KCS * 6;
 }
@@ -1068,6 +1098,17 @@ template <typename R> void launch_synth(const SD<R>& d, cudaStream_t st) {
   const int NJG = (JH + JG - 1) / JG;
   int nt = HV * NJG * KC;
   nt = nt > SY_THREADS ? SY_THREADS : ((nt + 31) / 32) * 32;
+  if constexpr (sizeof(R) == 4) {
+    if (d.legendre) {
+      // level fields on the tensor cores, surface fields by the FMA kernel
+      const StcPlan pl = stc_plan(d.E, d.J, d.K, d.N);
+      k_synth_tc<<<persistent_grid((const void*)k_synth_tc, STC_THREADS, pl.smem, pl.nunits),
+                   STC_THREADS, pl.smem, st>>>(d, d.tc_synth, pl, d.legendre);
+      k_synth<R, JG, KC, HV, true><<<dim3(NP, (d.E + SURF_EB - 1) / SURF_EB, 1), nt,
+                                       synth_smem<R>(NRmax, JH), st>>>(d);
+      return;
+    }
+  }
   k_synth<R, JG, KC, HV><<<dim3(NP, d.E, (d.K + KC - 1) / KC), nt, synth_smem<R>(NRmax, JH),
                            st>>>(d);
 }
@@ -1175,6 +1216,16 @@ template <typename R, int I> void set_attrs(const SD<R>& d) {
   cudaFuncSetAttribute(k_synth<R, Cfg<R>::JG, Cfg<R>::KCS, Cfg<R>::SHV>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)synth_smem<R>(NRmax, JH));
+  cudaFuncSetAttribute(k_synth<R, Cfg<R>::JG, Cfg<R>::KCS, Cfg<R>::SHV, true>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)synth_smem<R>(NRmax, JH));
+  if constexpr (sizeof(R) == 4) {
+    if (d.legendre) {
+      const StcPlan pl = stc_plan(d.E, d.J, d.K, d.N);
+      cudaFuncSetAttribute(k_synth_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
+      persistent_grid((const void*)k_synth_tc, STC_THREADS, pl.smem, 1);
+    }
+  }
 }
 
 template <typename R> int validate(const SD<R>& d) {
@@ -1196,9 +1247,11 @@ template <typename R> int validate(const SD<R>& d) {
     // tensor-core analysis: FP32 state, 16-latitude steps, 16-byte af rows,
     // at most 256 table rows, the plan within shared memory
     if (sizeof(R) != 4 || (d.legendre != 3 && d.legendre != 6) || !d.tc_anal ||
-        (d.J % 16) || (d.K & 1) || d.M > 256 ||
+        !d.tc_synth || (d.J % 16) || (d.K & 1) || d.M > 256 ||
         atc_plan(d.E, d.J, d.K, d.N).smem > 227 * 1024 ||
-        ((uintptr_t)d.tc_anal & 15))
+        stc_plan(d.E, d.J, d.K, d.N).smem > 227 * 1024 ||
+        (stc_plan(d.E, d.J, d.K, d.N).JT % 16) ||
+        ((uintptr_t)d.tc_anal & 15) || ((uintptr_t)d.tc_synth & 15))
       return LBM_ERR_ARG;
   }
   if (sizeof(R) == 4 &&

@@ -42,14 +42,18 @@ LBM_D void mbar_expect_tx(unsigned bar, unsigned bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes)
                : "memory");
 }
+// One poll.  A thread whose phase is not complete yet is suspended until it
+// completes or about TC_SUSPEND_NS pass (a hint), so waiting warps do not
+// spin on the issue slots the working warps need.
+constexpr unsigned TC_SUSPEND_NS = 1000000u;
 LBM_D bool mbar_try_wait(unsigned bar, unsigned parity) {
   unsigned ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}\n"
       : "=r"(ok)
-      : "r"(bar), "r"(parity)
+      : "r"(bar), "r"(parity), "r"(TC_SUSPEND_NS)
       : "memory");
   return ok != 0;
 }
@@ -66,8 +70,7 @@ LBM_D bool mbar_wait(unsigned bar, unsigned parity, int* err, int code) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = globaltimer_ns();
   for (;;) {
-    for (int i = 0; i < 256; ++i)
-      if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_try_wait(bar, parity)) return true;
     if (globaltimer_ns() - t0 > TC_WAIT_NS) break;
   }
   if (err) atomicOr(err, code);
@@ -80,8 +83,7 @@ LBM_D bool warp_wait(unsigned bar, unsigned parity, int* err, int code) {
   if (__all_sync(0xffffffffu, mbar_try_wait(bar, parity))) return true;
   const unsigned long long t0 = globaltimer_ns();
   for (;;) {
-    for (int i = 0; i < 256; ++i)
-      if (__all_sync(0xffffffffu, mbar_try_wait(bar, parity))) return true;
+    if (__all_sync(0xffffffffu, mbar_try_wait(bar, parity))) return true;
     const int late = globaltimer_ns() - t0 > TC_WAIT_NS ? 1 : 0;
     if (__shfl_sync(0xffffffffu, late, 0)) break;
   }
@@ -182,17 +184,29 @@ LBM_D Split3 split3(float x) {
   s.p[2] = __float2bfloat16_rn(r2);
   return s;
 }
+// The same split of two values at once (packed conversions): w[p] holds
+// piece p of a in its low and of b in its high 16 bits.
+LBM_D void split3_pair(float a, float b, unsigned* w) {
+  const __nv_bfloat162 h0 = __floats2bfloat162_rn(a, b);
+  const float2 f0 = __bfloat1622float2(h0);
+  const float ra = a - f0.x, rb = b - f0.y;
+  const __nv_bfloat162 h1 = __floats2bfloat162_rn(ra, rb);
+  const float2 f1 = __bfloat1622float2(h1);
+  const __nv_bfloat162 h2 = __floats2bfloat162_rn(ra - f1.x, rb - f1.y);
+  w[0] = *reinterpret_cast<const unsigned*>(&h0);
+  w[1] = *reinterpret_cast<const unsigned*>(&h1);
+  w[2] = *reinterpret_cast<const unsigned*>(&h2);
+}
 // Eight values along K -> three 16-byte rows (one per piece) of a tile.
 LBM_D void split3_store8(const float* x, unsigned char* row0, unsigned char* row1,
                          unsigned char* row2) {
   unsigned u[3][4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    const Split3 a = split3(x[2 * q]), b = split3(x[2 * q + 1]);
+    unsigned w[3];
+    split3_pair(x[2 * q], x[2 * q + 1], w);
 #pragma unroll
-    for (int p = 0; p < 3; ++p)
-      u[p][q] = (unsigned)__bfloat16_as_ushort(a.p[p]) |
-                ((unsigned)__bfloat16_as_ushort(b.p[p]) << 16);
+    for (int p = 0; p < 3; ++p) u[p][q] = w[p];
   }
   *reinterpret_cast<uint4*>(row0) = make_uint4(u[0][0], u[0][1], u[0][2], u[0][3]);
   *reinterpret_cast<uint4*>(row1) = make_uint4(u[1][0], u[1][1], u[1][2], u[1][3]);

@@ -309,6 +309,22 @@ class LBM:
 
     def _unload_stepper(self, stp):
         stp.flush()
+        if stp.precision != "fp64":
+            # FP32 state: the grid levels from the stepper's own synthesis
+            # kernels (previous level first: the current one leaves the
+            # stepper primed)
+            gb = stp.grid_level("b")
+            ga = stp.grid_level("a")
+            psa, psb = stp.psa.to(torch.float64), stp.psb.to(torch.float64)
+            if not self.batched:
+                ga = {k: v[0] for k, v in ga.items()}
+                gb = {k: v[0] for k, v in gb.items()}
+                psa, psb = psa[0], psb[0]
+            for st, g, ps in ((self.ga, ga, psa), (self.gb, gb, psb)):
+                st.u, st.v, st.t, st.q = g["u"], g["v"], g["t"], g["q"]
+                st.ps = ps.clone()
+            self.dyn.diag = {}
+            return
         a, b = stp.spectral_state()
         if not self.batched:
             a = {k: v[0] for k, v in a.items()}

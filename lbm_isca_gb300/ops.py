@@ -429,7 +429,7 @@ STEP_STATE = ("sa3", "sas", "sb3", "psa", "psb", "err", "err_member")
 STEP_WORK = ("sf", "sfs", "af", "afs", "tend", "tends", "grid6", "grid9")
 STEP_OPS = ("symp", "symh", "tw", "jfac", "vert", "b3", "bsd", "b2", "lap", "invlap", "nn1a",
             "kv", "kd", "ktt", "kq", "ww", "tmtx", "minv", "vdiff", "frc3", "frcs", "dft",
-            "tc_anal")
+            "tc_anal", "tc_synth")
 STEP_DIMS = ("prec", "nmem", "nlat", "nlon", "nmax", "kmax", "nsets", "strictly_linear",
              "vd_on0", "vd_on1", "vd_on2", "vd_on3", "frc_shared", "legendre")
 
@@ -554,8 +554,31 @@ def _(cur, prev, acc, w, mode):
     return None
 
 
+@torch.library.custom_op(f"{NS_}::link_copy_", mutates_args=("dst",))
+def link_copy_(dst: Tensor, src: Tensor) -> None:
+    """dst <- src (same shape and dtype, contiguous) by SM loads and stores
+    over the CPU-GPU link (lbm_link_copy); each tensor on the GPU or in
+    pinned host memory."""
+    if dst.shape != src.shape or dst.dtype != src.dtype:
+        raise ValueError("link_copy_: shapes and dtypes must match")
+    _w(dst)
+    if not src.is_contiguous():
+        raise ValueError("link_copy_: src must be contiguous")
+    if dst.device.type == "cpu" and not dst.is_pinned():
+        raise ValueError("link_copy_: host tensors must be pinned")
+    if src.device.type == "cpu" and not src.is_pinned():
+        raise ValueError("link_copy_: host tensors must be pinned")
+    check(lib().lbm_link_copy(_p(dst), _p(src), dst.numel() * dst.element_size(), _st()),
+          "lbm_link_copy")
+
+
+@link_copy_.register_fake
+def _(dst, src):
+    return None
+
+
 OPS = ("gauss_legendre", "legendre_tables", "fft_twiddles", "gravity_wave_matrices",
        "batched_inverse", "fourier_forward", "fourier_inverse", "legendre_analysis",
        "legendre_synthesis", "tendency_grid", "implicit_step", "tendency_grid_adjoint",
        "implicit_step_adjoint", "stepper_run", "stepper_prime", "stepper_colsum",
-       "stepper_flush", "history_accumulate")
+       "stepper_flush", "history_accumulate", "link_copy_")

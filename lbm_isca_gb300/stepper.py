@@ -59,6 +59,42 @@ def tc_anal_image(P, H, nn1a, N):
     return torch.cat(out).contiguous()
 
 
+def tc_synth_image(P, H, invlap, N):
+    """Table image of the tensor-core Legendre synthesis (the tc_synth layout
+    of include/lbm_gb300.h): per m, per latitude part (JT = J latitudes, or
+    J / 2 when six regions of J columns exceed the tensor memory), per step
+    of 16 rows n, the tables m P il, -H il, H il and P (il the inverse
+    Laplacian factor of row n) as JT x 16 tiles (rows = latitudes, K = n),
+    each split from FP64 into three bfloat16 pieces."""
+    J = P.shape[-1]
+    nparts = 1 if 6 * J <= 512 else 2
+    JT = J // nparts
+    P = P.to(torch.float64)
+    H = H.to(torch.float64)
+    il = invlap.to(torch.float64)
+    out = []
+    for m in range(N + 1):
+        nr = N + 1 - m
+        ks = (nr + 15) // 16
+        Pm, Hm, ilm = P[m, m:, :], H[m, m:, :], il[m:, None]
+        T = torch.zeros((4, ks * 16, J), device=P.device, dtype=torch.float64)
+        T[0, :nr] = m * Pm * ilm
+        T[1, :nr] = -Hm * ilm
+        T[2, :nr] = Hm * ilm
+        T[3, :nr] = Pm
+        for part in range(nparts):
+            X = T[:, :, part * JT:(part + 1) * JT].permute(0, 2, 1)     # [t][j][n]
+            pieces, r = [], X
+            for _ in range(3):
+                b = r.to(torch.bfloat16)
+                pieces.append(b.view(torch.int16))
+                r = r - b.to(torch.float64)
+            x = torch.stack(pieces, 1)                                # [t][p][JT][ks*16]
+            x = x.reshape(4, 3, JT // 8, 8, ks, 2, 8)                  # [t][p][rg][r8][s][kc][k8]
+            out.append(x.permute(4, 0, 1, 2, 5, 3, 6).reshape(-1))
+    return torch.cat(out).contiguous()
+
+
 class EnsembleStepper:
     """Fused GPU time stepping of `nmem` members sharing one basic state."""
 
@@ -148,6 +184,8 @@ class EnsembleStepper:
         self.af, self.afs = z(E, M, J, K, 7), z(E, M, J, 2)
         self.tend, self.tends = z(E, 4, NS, K), z(E, 2, NS)
         self.tc_anal = self._tc_anal_image() if self.legendre else None
+        self.tc_synth = (tc_synth_image(sp.pnm, sp.hnm, sp.inv_laplace, N)
+                         if self.legendre else None)
         # FP32 grid rows between the longitude transforms and the column algebra
         if precision != "fp64":
             f = lambda *s_: torch.zeros(s_, device=dev, dtype=torch.float32)   # noqa: E731
@@ -328,6 +366,7 @@ class EnsembleStepper:
         d.err_member = C.cast(C.c_void_p(self.err_member.data_ptr()), C.POINTER(C.c_int))
         d.legendre = self.legendre
         d.tc_anal = ptr(self.tc_anal)
+        d.tc_synth = ptr(self.tc_synth)
         self._desc = d
         return d
 
@@ -466,6 +505,34 @@ class EnsembleStepper:
         state was loaded (the per-member flags k_implicit sets)."""
         self.stream.synchronize()
         return torch.nonzero(self.err_member).flatten().tolist()
+
+    def grid_level(self, level):
+        """Grid u, v, T, q ([E][J][I][K], FP64) of the current level ("a") or
+        of the filtered previous level ("b"), from the stepper's own FP32
+        synthesis kernels (Legendre synthesis into sf, then the longitude
+        synthesis into grid6) -- FP32 state only.  Synthesising "a" leaves
+        sf as priming left it, so "b" is taken first when both are wanted."""
+        if self.precision == "fp64":
+            raise ValueError("grid_level needs an FP32-state stepper")
+        d = StepperDesc.from_buffer_copy(self.desc())
+        if level == "b":
+            d.sa3 = ptr(self.sb3)
+        ctl = self._ctl([(self._dts[0], False, 0)])
+        s = stream_handle(self.stream)
+        E, J, I, K = self.E, self.J, self.I, self.K
+        self.stream.wait_stream(torch.cuda.default_stream(self.dev))
+        with torch.cuda.stream(self.stream):
+            for kern in (3, 4):          # Legendre synthesis, longitude synthesis
+                check(lib().lbm_stepper_launch(C.byref(d), ctl, kern, s),
+                      "lbm_stepper_launch")
+            rows = self.grid6.view(E, J, 6 + 6 * K, I)[:, :, 6:].view(E, J, K, 6, I)
+            out = {}
+            for f, name in ((0, "u"), (1, "v"), (4, "t"), (5, "q")):
+                t = torch.empty((E, J, I, K), device=self.dev, dtype=torch.float64)
+                t.copy_(rows[:, :, :, f, :].permute(0, 1, 3, 2))
+                out[name] = t
+        torch.cuda.default_stream(self.dev).wait_stream(self.stream)
+        return out
 
     def snapshot(self):
         """Copy of the current level (rectangle dict incl. pi)."""

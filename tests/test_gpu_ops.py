@@ -231,3 +231,24 @@ def test_adjoint_operators_dot_product(torch):
     rhs = state_dot(da, a1) + state_dot(db, a2)
     assert abs(lhs - rhs) / abs(lhs) < 1e-10
     assert {"tendency_grid_adjoint", "implicit_step_adjoint", "tendency_grid"} <= log.names
+
+
+@pytest.mark.parametrize("n", [1, 13, 4096, 1000003])
+def test_link_copy_round_trip(torch, n):
+    """lbm_link_copy (link_copy_): pinned host -> device -> pinned host, any
+    length, bit for bit; pageable host memory is refused."""
+    src = torch.arange(n, dtype=torch.float64).mul_(1.0 / 3.0).pin_memory()
+    dev = torch.empty(n, dtype=torch.float64, device="cuda")
+    back = torch.empty(n, dtype=torch.float64).pin_memory()
+    torch.ops.lbm_gb300.link_copy_(dev, src)
+    torch.ops.lbm_gb300.link_copy_(back, dev)
+    torch.cuda.synchronize()
+    assert torch.equal(back, src)
+    assert torch.equal(dev.cpu(), src)
+    b8 = torch.arange(n, dtype=torch.uint8).pin_memory()
+    d8 = torch.empty(n, dtype=torch.uint8, device="cuda")
+    torch.ops.lbm_gb300.link_copy_(d8, b8)
+    torch.cuda.synchronize()
+    assert torch.equal(d8.cpu(), b8)
+    with pytest.raises(ValueError):
+        torch.ops.lbm_gb300.link_copy_(torch.empty(n, dtype=torch.float64), dev)

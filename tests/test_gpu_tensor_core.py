@@ -1,7 +1,7 @@
-"""The Legendre analysis on the tensor cores (tcgen05, bfloat16 split
-operands, FP32 accumulation in tensor memory) against an FP64 numpy
-restatement of the same contraction, next to the FP32 FMA kernel it
-replaces; and whole runs in the bf16 modes against the FP64 path."""
+"""The Legendre analysis and synthesis on the tensor cores (tcgen05,
+bfloat16 split operands, FP32 accumulation in tensor memory) against FP64
+numpy restatements of the same contractions, next to the FP32 FMA kernels
+they replace; and whole runs in the bf16 modes against the FP64 path."""
 
 import ctypes as C
 
@@ -90,6 +90,67 @@ def test_analysis_kernel_vs_fp64(torch, case):
     errs = {p: float(np.linalg.norm(g - ref) / np.linalg.norm(ref)) for p, g in got.items()}
     # the tensor-core surface part is the FMA kernel's own code
     assert np.array_equal(tends["bf16x3"], tends["fp32"])
+    assert errs["fp32"] < 2e-6, errs
+    assert errs["bf16x3"] < max(2e-6, 3 * errs["fp32"]), errs
+    assert errs["bf16split"] < 1e-3, errs
+
+
+def _oracle_synthesis(tr, sa3, K):
+    """sf [E][M][J][K][6] of the packed state sa3 [E][4][NS][K] in FP64:
+    U = i m P il div - H il vor, V = i m P il vor + H il div, then P vor,
+    P div, P T, P q (sums over n = m..N, every latitude)."""
+    E = sa3.shape[0]
+    M = tr.nmax + 1
+    il = tr.invlap
+    out = np.zeros((E, M, tr.nlat, K, 6), dtype=np.complex128)
+    off = 0
+    for m in range(M):
+        nr = M - m
+        sl = slice(off, off + nr)
+        P, H, ilm = tr.P[m, m:, :], tr.H[m, m:, :], il[m:, None]
+        for e in range(E):
+            vo, dv, tt, qq = (sa3[e, f, sl] for f in range(4))       # [n][k]
+            S = lambda T, x: T.T @ x                                   # noqa: E731 [j][k]
+            out[e, m, :, :, 0] = 1j * m * S(P, ilm * dv) - S(H, ilm * vo)
+            out[e, m, :, :, 1] = 1j * m * S(P, ilm * vo) + S(H, ilm * dv)
+            out[e, m, :, :, 2] = S(P, vo)
+            out[e, m, :, :, 3] = S(P, dv)
+            out[e, m, :, :, 4] = S(P, tt)
+            out[e, m, :, :, 5] = S(P, qq)
+        off += nr
+    return out
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_synthesis_kernel_vs_fp64(torch, case):
+    from lbm_isca_gb300._lib import StepCtl, check, lib
+    from lbm_isca_gb300.backend import stream_handle
+    nlon, nlat, nmax, K, E = CASES[case]
+    tr = orc.SphericalTransform(nlon, nlat, nmax)
+    M = nmax + 1
+    NS = M * (M + 1) // 2
+    rng = np.random.default_rng(23)
+    sa3 = rng.normal(size=(E, 4, NS, K)) + 1j * rng.normal(size=(E, 4, NS, K))
+    sa3[:, :, :M] = sa3[:, :, :M].real          # m = 0 rows are real
+    sas = rng.normal(size=(E, 4, NS)) + 1j * rng.normal(size=(E, 4, NS))
+    ref = _oracle_synthesis(tr, sa3, K)
+    got, sfs = {}, {}
+    for prec in ("fp32", "bf16x3", "bf16split"):
+        stp = _stepper(torch, case, prec)
+        stp.sa3.copy_(torch.as_tensor(sa3, device="cuda").to(torch.complex64))
+        stp.sas.copy_(torch.as_tensor(sas, device="cuda").to(torch.complex64))
+        stp.sf.zero_()
+        ctl = (StepCtl * 1)()
+        ctl[0].dt, ctl[0].set, ctl[0].ps_mode, ctl[0].ra_mode = 1200.0, 0, 0, 1
+        with torch.cuda.stream(stp.stream):
+            check(lib().lbm_stepper_launch(C.byref(stp.desc()), ctl, 3,
+                                           stream_handle(stp.stream)), "synthesis")
+        stp.stream.synchronize()
+        assert int(stp.err.item()) == 0
+        got[prec] = stp.sf.cpu().numpy().astype(np.complex128)
+        sfs[prec] = stp.sfs.cpu().numpy()
+    errs = {p: float(np.linalg.norm(g - ref) / np.linalg.norm(ref)) for p, g in got.items()}
+    assert np.array_equal(sfs["bf16x3"], sfs["fp32"])
     assert errs["fp32"] < 2e-6, errs
     assert errs["bf16x3"] < max(2e-6, 3 * errs["fp32"]), errs
     assert errs["bf16split"] < 1e-3, errs

@@ -206,6 +206,45 @@ def test_tensor_core_table_image_layout():
             off = (r // 8) * 128 + (kk // 8) * 64 + (r % 8) * 8 + kk % 8
             val = sum(bf16(img[tile + (t * 3 + p) * nb * 16 + off]) for p in range(3))
             ref = tabs[t][m, m + r, s * 16 + kk] if r < nr else 0.0
-            assert abs(val - ref) <= 2.0 ** -24 * abs(ref) + 1e-300, (m, s, t, r, kk)
+            assert abs(val - ref) <= 2.0 ** -24 * abs(ref) + 1e-36, (m, s, t, r, kk)
         base += KS * 9 * nb * 16
     assert base == img.size
+
+
+def test_tensor_core_synthesis_table_image_layout():
+    """The tc_synth table image: (m, part, step) blocks in order, the tables
+    m P il, -H il, H il, P as latitude x 16-row tiles, pieces summing to the
+    FP64 values (checked on the CPU against the oracle's tables)."""
+    import torch
+    from oracle import lbm_oracle as orc
+    from lbm_isca_gb300.stepper import tc_synth_image
+    for (nlon, nlat, N) in ((64, 32, 21), (256, 128, 85)):
+        tr = orc.SphericalTransform(nlon, nlat, N)
+        J = nlat
+        nparts = 1 if 6 * J <= 512 else 2
+        JT = J // nparts
+        il = tr.invlap
+        img = tc_synth_image(torch.as_tensor(tr.P), torch.as_tensor(tr.H),
+                             torch.as_tensor(il), N).numpy().view(np.uint16)
+
+        def bf16(u):
+            return (u.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+        rng = np.random.default_rng(1)
+        base = 0
+        for m in range(N + 1):
+            nr = N + 1 - m
+            ks = (nr + 15) // 16
+            tabs = (m * tr.P[m] * il[:, None], -tr.H[m] * il[:, None], tr.H[m] * il[:, None],
+                    tr.P[m])
+            for part in range(nparts):
+                for _ in range(12):
+                    s, t = rng.integers(ks), rng.integers(4)
+                    r, kk = rng.integers(JT), rng.integers(16)
+                    n = m + 16 * s + kk
+                    blk = base + (part * ks + s) * 12 * JT * 16
+                    off = (r // 8) * 128 + (kk // 8) * 64 + (r % 8) * 8 + kk % 8
+                    val = sum(bf16(img[blk + (t * 3 + p) * JT * 16 + off]) for p in range(3))
+                    ref = tabs[t][n, part * JT + r] if n <= N else 0.0
+                    assert abs(val - ref) <= 2.0 ** -24 * abs(ref) + 1e-36, (m, part, s, t, r)
+            base += nparts * ks * 12 * JT * 16
+        assert base == img.size
