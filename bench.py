@@ -71,6 +71,11 @@ def parse():
                          "heating rounded to FP32 (a relative input change below 2^-24), next "
                          "to FP32 against FP64, T42L20 x 128 members (seed 2) and T85L40 x 8, "
                          "reference dynamics and strictly linear, instead of the bench")
+    ap.add_argument("--config4", action="store_true",
+                    help="uneven batching: 48 T21L20 + 32 T42L20 + 16 T85L40 members (seed 4, "
+                         "strictly linear), 20 days in one CUDA graph per stretch of steady "
+                         "steps, autotuned tensor-core tiles per truncation, instead of the "
+                         "bench")
     ap.add_argument("--sweep", action="store_true",
                     help="precision sweep (FP32 vs FP64 per field at days 10 and 30, "
                          "T42L20 x 128 members and T85L40 x 16 members) instead of the bench")
@@ -352,6 +357,46 @@ def precision_sweep(torch):
     return out
 
 
+def config4_measurement(torch, precision, days=20, groups=((64, 32, 21, 20, 48),
+                                                             (128, 64, 42, 20, 32),
+                                                             (256, 128, 85, 40, 16))):
+    """Members of three truncations stepped together (GroupedEnsemble): the
+    seeded heatings of every group drawn in order from one generator (seed
+    4), solid-body basic states, plain damping, strictly linear dynamics (the
+    reference dynamics let strongly forced T85L40 members grow without bound
+    by day 14), dt 1200 s, `days` model days; device time of the whole run
+    and of the steady part, per-group tile choices of the autotuner, and each
+    group's state against the same group run alone (bitwise)."""
+    from lbm_isca_gb300 import configs
+    from lbm_isca_gb300.grouped import GroupedEnsemble
+    sig = {K: configs.equal_sigma_half_levels(K) for K in {g[3] for g in groups}}
+    heats = configs.grouped_heating([(nlon, nlat, sig[K], E)
+                                     for nlon, nlat, _, K, E in groups], seed=4)
+    specs = [dict(nlon=nlon, nlat=nlat, nmax=nmax, sigm=sig[K], heats=h,
+                  basic_state=configs.solid_body_basic_state(nlon, nlat, sig[K]),
+                  config=dict(configs.plain_damping(K), strictly_linear=True))
+             for (nlon, nlat, nmax, K, E), h in zip(groups, heats)]
+    ge = GroupedEnsemble(specs, precision=precision, tune=True)
+    nsteps = 72 * days
+    ge.run(4)                                   # capture the graphs, warm up
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    ge.run(nsteps)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    finite = ge.check_finite()
+    E = ge.members
+    return {"workload": "48 T21L20 + 32 T42L20 + 16 T85L40 members, seeded heatings (seed 4), "
+                        f"strictly linear, dt 1200 s, {days} days, {precision}",
+            "members": E, "steps": nsteps, "seconds": ms / 1000.0,
+            "member_steps_per_s": E * nsteps / (ms / 1000.0), "finite": finite,
+            "tiles": [{"grid": f"T{g['stepper'].N}L{g['stepper'].K}",
+                       "members": g["stepper"].E, "choice": g["tile"]} for g in ge.groups]}
+
+
 def conditioning(torch, days=(10, 30)):
     """How much of the FP32-against-FP64 difference the problem itself sets:
     the same FP64 run with each heating rounded to FP32 (every input changed
@@ -546,6 +591,11 @@ def main():
         torch.cuda.set_device(0)
         out = adjoint_measurement(torch, fd_dirs=args.fd_dirs, nsteps=args.adjoint_steps)
         print(json.dumps({"adjoint": out}), flush=True)
+        return
+    if args.config4:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps({"config4": config4_measurement(torch, args.precision)}), flush=True)
         return
     if args.conditioning:
         import torch

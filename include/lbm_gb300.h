@@ -279,6 +279,11 @@ int lbm_implicit_step_adjoint(int prec, const lbm_implicit_adj_args* a, void* st
  *        n (zero for n = 0; rows past N are zero), each as three bfloat16
  *        pieces, each piece a JT x 16 tile (rows = latitudes of the part,
  *        K = kk) in the layout of tc_anal
+ *   tc_off: with legendre != 0, bit 0 keeps the analysis and bit 1 the
+ *        synthesis on the FMA kernels (0 = both on the tensor cores)
+ *   tc_g: at most this many members per 128-lane MMA tile of the tensor-core
+ *        kernels (0 = as many as fit, 128 / (2 kmax)); fewer members make
+ *        more, smaller units of work (a choice of the tile autotuner)
  * sf, af and grid9 must be 16-byte aligned (LBM_ERR_ARG otherwise).
  * ==========================================================================*/
 enum {
@@ -303,6 +308,8 @@ typedef struct lbm_stepper_desc {
   int legendre;
   const void* tc_anal;
   const void* tc_synth;
+  int tc_off;
+  int tc_g;
 } lbm_stepper_desc;
 
 /* Per-step control.  dt: time step of this call; set: which operator set

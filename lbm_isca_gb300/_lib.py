@@ -78,7 +78,8 @@ class StepperDesc(C.Structure):
                                      "sb3", "psa", "psb", "sf", "sfs", "af", "afs", "tend",
                                      "tends", "grid6", "grid9")]
                 + [("err", C.POINTER(I32)), ("err_member", C.POINTER(I32)),
-                   ("legendre", I32), ("tc_anal", VP), ("tc_synth", VP)])
+                   ("legendre", I32), ("tc_anal", VP), ("tc_synth", VP), ("tc_off", I32),
+                   ("tc_g", I32)])
 
 
 class StepCtl(C.Structure):

@@ -1,0 +1,124 @@
+"""Tile autotuner of the tensor-core Legendre kernels.
+
+For a stepper in a tensor-core precision ("bf16x3", "bf16split") the
+choices are, per transform direction, the tensor-core kernel or the FP32 FMA
+kernel (both FP32-level in bf16x3), and the members per 128-lane MMA tile
+(the tile's M extent: (members, level, Re|Im) rows; fewer members give more,
+smaller units of work, which pays for small ensembles).  On first use of a
+(GPU, grid, levels, members, precision) each candidate's analysis and
+synthesis launches are timed with CUDA events on the stepper's stream and the
+fastest is kept in a JSON cache (``$LBM_AUTOTUNE_CACHE``, by default
+``lbm_isca_gb300/_lib/autotune.json`` next to the library); later steppers of
+the same shape read the choice from it.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import tempfile
+
+import torch
+
+from ._lib import LIBPATH, StepCtl, check, lib
+from .backend import stream_handle
+
+CACHE = os.environ.get("LBM_AUTOTUNE_CACHE",
+                       os.path.join(os.path.dirname(LIBPATH), "autotune.json"))
+
+
+def _key(stp):
+    name = torch.cuda.get_device_name(stp.dev)
+    return (f"{name}|J{stp.J} I{stp.I} N{stp.N} K{stp.K} E{stp.E}|{stp.precision}")
+
+
+def candidates(stp):
+    """(tc_off, tc_g) pairs: tc_off bit 0 = analysis on FMA, bit 1 =
+    synthesis on FMA; tc_g = members per MMA tile (0 = as many as fit)."""
+    gmax = max(1, min(128 // (2 * stp.K), stp.E))
+    gs = sorted({gmax, max(1, gmax // 2), 1}, reverse=True)
+    out = [(3, 0)]
+    for off in (0, 1, 2):
+        out += [(off, g) for g in gs]
+    return out
+
+
+def _apply(stp, off, g):
+    stp.tc_off, stp.tc_g = int(off), int(g)
+    stp._desc = None
+    stp._oargs = None
+
+
+def time_choice(stp, off, g, reps=5, warm=2):
+    """ms of one analysis + one synthesis launch with the given choice."""
+    _apply(stp, off, g)
+    ctl = (StepCtl * 1)()
+    ctl[0].dt, ctl[0].set, ctl[0].ps_mode, ctl[0].ra_mode = stp._dts[0], 0, 0, 1
+    s = stream_handle(stp.stream)
+    L = lib()
+    d = stp.desc()
+    with torch.cuda.stream(stp.stream):
+        for _ in range(warm):
+            for kern in (1, 3):
+                check(L.lbm_stepper_launch(C.byref(d), ctl, kern, s), "lbm_stepper_launch")
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stp.stream)
+        for _ in range(reps):
+            for kern in (1, 3):
+                check(L.lbm_stepper_launch(C.byref(d), ctl, kern, s), "lbm_stepper_launch")
+        e1.record(stp.stream)
+    stp.stream.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def _load(path):
+    try:
+        with open(path) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(path, cache):
+    d = os.path.dirname(path)
+    os.makedirs(d, exist_ok=True)
+    fd, tmp = tempfile.mkstemp(dir=d, suffix=".tmp")
+    with os.fdopen(fd, "w") as fh:
+        json.dump(cache, fh, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+
+
+def tune(stp, force=False, path=None):
+    """Choose and apply the fastest tile choice for this stepper (a no-op for
+    the FP64 and FP32 precisions); returns the cache record.  The timed
+    launches overwrite only the intermediates, which are restored, so the
+    stepper may hold a loaded state."""
+    if not stp.legendre:
+        return None
+    path = path or CACHE
+    cache = _load(path)
+    key = _key(stp)
+    rec = cache.get(key)
+    if rec is not None and not force:
+        _apply(stp, rec["tc_off"], rec["tc_g"])
+        return rec
+    if not stp._dts:
+        stp.set_timesteps([1200.0])
+    torch.cuda.default_stream(stp.dev).wait_stream(stp.stream)
+    keep = {n: getattr(stp, n).clone() for n in ("sf", "sfs", "af", "afs", "tend", "tends")}
+    times = {}
+    for off, g in candidates(stp):
+        times[f"{off},{g}"] = time_choice(stp, off, g)
+    best = min(times, key=times.get)
+    off, g = (int(x) for x in best.split(","))
+    _apply(stp, off, g)
+    with torch.cuda.stream(stp.stream):
+        for n, t in keep.items():
+            getattr(stp, n).copy_(t)
+    stp.stream.synchronize()
+    rec = {"tc_off": off, "tc_g": g, "ms": times[best], "candidates_ms": times}
+    cache[key] = rec
+    _store(path, cache)
+    return rec

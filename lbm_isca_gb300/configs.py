@@ -124,6 +124,29 @@ def ensemble_heating(nlon, nlat, sigm, nmem, seed):
     return out, params
 
 
+def grouped_heating(groups, seed=4):
+    """Seeded heatings of an uneven ensemble (the mixed-truncation
+    configuration): one generator draws the members of every group in order
+    (all of the first group, then the second, ...), each member's centre
+    (lon U(0, 360), lat U(-15, 15)), amplitude (lognormal, median 2 K/day,
+    sigma 0.5) and peak sigma (U(0.3, 0.6)) as ensemble_heating draws them.
+    groups: [(nlon, nlat, sigm, nmem)]; returns a list of (nmem, nlat, nlon,
+    K) arrays in K/s."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for nlon, nlat, sigm, nmem in groups:
+        h = np.empty((nmem, nlat, nlon, len(sigm) - 1))
+        for e in range(nmem):
+            lon0 = rng.uniform(0.0, 360.0)
+            lat0 = rng.uniform(-15.0, 15.0)
+            amp = rng.lognormal(math.log(2.0), 0.5)
+            sp = rng.uniform(0.3, 0.6)
+            h[e] = elliptic_heating(nlon, nlat, sigm, lon0=lon0, lat0=lat0, amp_k_per_day=amp,
+                                    sigma_peak=sp)
+        out.append(h)
+    return out
+
+
 def plain_damping(K):
     """Config keywords of the plain configuration's damping."""
     drag = [1.0] + [30.0] * (K - 2) + [1.0]

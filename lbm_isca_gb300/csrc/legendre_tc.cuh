@@ -34,7 +34,6 @@
 // the CTA winds down without leaving copies or MMAs in flight.
 #pragma once
 #include "tc_common.cuh"
-#include "async_copy.cuh"
 
 namespace lbm {
 
@@ -44,7 +43,6 @@ constexpr int ATC_CONV_WARPS = 16;     // two groups of 8: even / odd A matrices
 constexpr int ATC_THREADS = 32 * (2 + ATC_CONV_WARPS + 4);
 constexpr int ATC_NMAT = 9;
 constexpr int ATC_ERR = 2;            // *err bit set by a timed-out wait
-constexpr unsigned ATC_PREFETCH = 6;  // steps of af rows pulled into L2 ahead
 
 LBM_HD int atc_nb(int N, int m) { return ((N + 1 - m) + 15) / 16 * 16; }
 
@@ -54,9 +52,12 @@ struct AtcPlan {
   unsigned data_bytes, tab_bytes, stage_bytes, a_bytes, smem;
 };
 
-LBM_HD AtcPlan atc_plan(int E, int J, int K, int N) {
+// gcap > 0 caps the members per MMA tile (a tuning choice: fewer members,
+// more units of work).
+LBM_HD AtcPlan atc_plan(int E, int J, int K, int N, int gcap = 0) {
   AtcPlan p;
   p.G = 128 / (2 * K);
+  if (gcap > 0 && p.G > gcap) p.G = gcap;
   if (p.G < 1) p.G = 1;
   if (p.G > E) p.G = E;
   p.ngroups = (E + p.G - 1) / p.G;
@@ -216,19 +217,6 @@ __global__ void __launch_bounds__(ATC_THREADS, 1)
     if (lane == 0) {
       unsigned t = 0;
       const unsigned rowb = (unsigned)(16 * K * 7 * 8);
-      // the af rows of step t (the t-th step of this CTA's units) pulled into
-      // L2 ahead of their bulk copy, ATC_PREFETCH steps early
-      auto prefetch = [&](unsigned tp) {
-        const int u = blockIdx.x + (int)(tp / KS) * gridDim.x, s = (int)(tp % KS);
-        if (u >= pl.nunits) return;
-        const int m = u / pl.ngroups, g = u - m * pl.ngroups;
-        const int e0 = g * pl.G, gm = min(pl.G, E - e0);
-        for (int mi = 0; mi < gm; ++mi)
-          prefetch_l2_bulk(reinterpret_cast<const float*>(d.af) +
-                               ((((size_t)(e0 + mi) * M + m) * J + s * 16) * K) * 14,
-                           rowb);
-      };
-      for (unsigned tp = 0; tp < ATC_PREFETCH; ++tp) prefetch(tp);
       for (int u = blockIdx.x; u < pl.nunits && ok; u += gridDim.x) {
         const int m = u / pl.ngroups, g = u - m * pl.ngroups;
         const int e0 = g * pl.G, gm = min(pl.G, E - e0);
@@ -236,7 +224,6 @@ __global__ void __launch_bounds__(ATC_THREADS, 1)
         const unsigned tb = 9u * nb * 32u;
         const unsigned char* tm = tabs + atc_tab_offset(N, KS, m);
         for (int s = 0; s < KS && ok; ++s, ++t) {
-          prefetch(t + ATC_PREFETCH);
           const int st = t % ATC_STAGES;
           const unsigned ph = (t / ATC_STAGES) & 1u;
           ok = mbar_wait(smem_addr(&sm->empty[st]), ph ^ 1u, err, ATC_ERR);

@@ -53,6 +53,8 @@ template <typename R> struct SD {
   int legendre;                          // 0 FMA; 3 or 6: tensor-core products
   const unsigned char* tc_anal;          // table image of k_anal_tc
   const unsigned char* tc_synth;         // table image of k_synth_tc
+  int tc_off;                            // bit 0: analysis, bit 1: synthesis on FMA
+  int tc_g;                              // members per MMA tile cap (0: as many as fit)
 };
 
 template <typename R> SD<R> make_sd(const lbm_stepper_desc& d) {
@@ -81,6 +83,8 @@ template <typename R> SD<R> make_sd(const lbm_stepper_desc& d) {
   s.legendre = d.legendre;
   s.tc_anal = (const unsigned char*)d.tc_anal;
   s.tc_synth = (const unsigned char*)d.tc_synth;
+  s.tc_off = d.tc_off;
+  s.tc_g = d.tc_g;
   return s;
 }
 
@@ -1077,7 +1081,7 @@ template <typename R, int KC> void launch_anal(const SD<R>& d, cudaStream_t st, 
     cudaFuncSetAttribute(k_anal<R, NC, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     cudaFuncSetAttribute(k_anal<R, NC, KC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)sm);
-  } else if (d.legendre && sizeof(R) == 4) {
+  } else if (d.legendre && !(d.tc_off & 1) && sizeof(R) == 4) {
     k_anal<R, NC, KC, true><<<dim3(NP, (d.E + SURF_EB - 1) / SURF_EB, 1), nt, sm, st>>>(d);
   } else {
     k_anal<R, NC, KC><<<dim3(NP, d.E, (d.K + KC - 1) / KC), nt, sm, st>>>(d);
@@ -1099,9 +1103,9 @@ template <typename R> void launch_synth(const SD<R>& d, cudaStream_t st) {
   int nt = HV * NJG * KC;
   nt = nt > SY_THREADS ? SY_THREADS : ((nt + 31) / 32) * 32;
   if constexpr (sizeof(R) == 4) {
-    if (d.legendre) {
+    if (d.legendre && !(d.tc_off & 2)) {
       // level fields on the tensor cores, surface fields by the FMA kernel
-      const StcPlan pl = stc_plan(d.E, d.J, d.K, d.N);
+      const StcPlan pl = stc_plan(d.E, d.J, d.K, d.N, d.tc_g);
       k_synth_tc<<<persistent_grid((const void*)k_synth_tc, STC_THREADS, pl.smem, pl.nunits),
                    STC_THREADS, pl.smem, st>>>(d, d.tc_synth, pl, d.legendre);
       k_synth<R, JG, KC, HV, true><<<dim3(NP, (d.E + SURF_EB - 1) / SURF_EB, 1), nt,
@@ -1171,8 +1175,8 @@ template <typename R, int I> int launch_step(const SD<R>& d, const lbm_step_ctl&
   }
   if (only < 0 || only == 1) {
     if constexpr (sizeof(R) == 4) {
-      if (d.legendre) {
-        const AtcPlan pl = atc_plan(d.E, d.J, d.K, d.N);
+      if (d.legendre && !(d.tc_off & 1)) {
+        const AtcPlan pl = atc_plan(d.E, d.J, d.K, d.N, d.tc_g);
         k_anal_tc<<<persistent_grid((const void*)k_anal_tc, ATC_THREADS, pl.smem, pl.nunits),
                     ATC_THREADS, pl.smem, st>>>(d, d.tc_anal, pl, d.legendre);
       }
@@ -1206,7 +1210,7 @@ template <typename R, int I> void set_attrs(const SD<R>& d) {
   run_anal<R>(d, nullptr, true);
   if constexpr (sizeof(R) == 4) {
     if (d.legendre) {
-      const AtcPlan pl = atc_plan(d.E, d.J, d.K, d.N);
+      const AtcPlan pl = atc_plan(d.E, d.J, d.K, d.N, d.tc_g);
       cudaFuncSetAttribute(k_anal_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
       persistent_grid((const void*)k_anal_tc, ATC_THREADS, pl.smem, 1);
     }
@@ -1221,7 +1225,7 @@ template <typename R, int I> void set_attrs(const SD<R>& d) {
                        (int)synth_smem<R>(NRmax, JH));
   if constexpr (sizeof(R) == 4) {
     if (d.legendre) {
-      const StcPlan pl = stc_plan(d.E, d.J, d.K, d.N);
+      const StcPlan pl = stc_plan(d.E, d.J, d.K, d.N, d.tc_g);
       cudaFuncSetAttribute(k_synth_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
       persistent_grid((const void*)k_synth_tc, STC_THREADS, pl.smem, 1);
     }
@@ -1248,9 +1252,10 @@ template <typename R> int validate(const SD<R>& d) {
     // at most 256 table rows, the plan within shared memory
     if (sizeof(R) != 4 || (d.legendre != 3 && d.legendre != 6) || !d.tc_anal ||
         !d.tc_synth || (d.J % 16) || (d.K & 1) || d.M > 256 ||
-        atc_plan(d.E, d.J, d.K, d.N).smem > 227 * 1024 ||
-        stc_plan(d.E, d.J, d.K, d.N).smem > 227 * 1024 ||
-        (stc_plan(d.E, d.J, d.K, d.N).JT % 16) ||
+        atc_plan(d.E, d.J, d.K, d.N, d.tc_g).smem > 227 * 1024 ||
+        stc_plan(d.E, d.J, d.K, d.N, d.tc_g).smem > 227 * 1024 ||
+        (stc_plan(d.E, d.J, d.K, d.N).JT % 16) || d.tc_off < 0 || d.tc_off > 3 ||
+        d.tc_g < 0 ||
         ((uintptr_t)d.tc_anal & 15) || ((uintptr_t)d.tc_synth & 15))
       return LBM_ERR_ARG;
   }

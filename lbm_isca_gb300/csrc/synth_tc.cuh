@@ -23,7 +23,6 @@
 // FMA kernel (k_synth, surface part only).
 #pragma once
 #include "tc_common.cuh"
-#include "async_copy.cuh"
 
 namespace lbm {
 
@@ -34,7 +33,6 @@ constexpr int STC_THREADS = 32 * (2 + STC_CONV_WARPS + 4);
 constexpr int STC_NTILE = 6;          // vor, i vor, div, i div, T, q
 constexpr int STC_NTAB = 4;           // m P il, -H il, H il, P
 constexpr int STC_NREG = 6;           // U, V, VOR, DIV, T, Q
-constexpr int STC_PREFETCH = 6;       // steps of state rows pulled into L2 ahead
 
 LBM_HD int stc_ks(int N, int m) { return (N + 1 - m + 15) / 16; }
 
@@ -43,9 +41,10 @@ struct StcPlan {
   unsigned data_bytes, tab_bytes, stage_bytes, a_bytes, smem;
 };
 
-LBM_HD StcPlan stc_plan(int E, int J, int K, int N) {
+LBM_HD StcPlan stc_plan(int E, int J, int K, int N, int gcap = 0) {
   StcPlan p;
   p.G = 128 / (2 * K);
+  if (gcap > 0 && p.G > gcap) p.G = gcap;
   if (p.G < 1) p.G = 1;
   if (p.G > E) p.G = E;
   p.ngroups = (E + p.G - 1) / p.G;
@@ -184,27 +183,6 @@ __global__ void __launch_bounds__(STC_THREADS, 1)
       unsigned t = 0;
       const unsigned rowb = (unsigned)(K * 8);        // one (n) row of K complex
       const unsigned tb = pl.tab_bytes;
-      // a second cursor over this CTA's (unit, step) sequence, STC_PREFETCH
-      // steps ahead, pulls the state rows of that step into L2
-      int pu = blockIdx.x, ps = 0;
-      auto prefetch_next = [&]() {
-        if (pu >= pl.nunits) return;
-        int m, part, g;
-        unit(pu, m, part, g);
-        const int e0 = g * pl.G, gm = min(pl.G, E - e0);
-        const int nv = min(16, N + 1 - m - 16 * ps);
-        const size_t off = (size_t)spec_offset(m, N);
-        for (int mi = 0; mi < gm; ++mi)
-          for (int f = 0; f < 4; ++f)
-            prefetch_l2_bulk(reinterpret_cast<const float*>(d.sa3) +
-                                 ((((size_t)(e0 + mi) * 4 + f) * NS + off + 16 * ps) * K) * 2,
-                             nv * rowb);
-        if (++ps == stc_ks(N, m)) {
-          ps = 0;
-          pu += gridDim.x;
-        }
-      };
-      for (int i = 0; i < STC_PREFETCH; ++i) prefetch_next();
       for (int u = blockIdx.x; u < pl.nunits && ok; u += gridDim.x) {
         int m, part, g;
         unit(u, m, part, g);
@@ -213,7 +191,6 @@ __global__ void __launch_bounds__(STC_THREADS, 1)
         const unsigned char* tm = tabs + stc_tab_offset(N, pl.nparts, JT, m, part);
         const size_t off = (size_t)spec_offset(m, N);
         for (int s = 0; s < ks && ok; ++s, ++t) {
-          prefetch_next();
           const int st = t % STC_STAGES;
           ok = mbar_wait(smem_addr(&sm->empty[st]), ((t / STC_STAGES) & 1u) ^ 1u, err, ATC_ERR);
           if (!ok) break;

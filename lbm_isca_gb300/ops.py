@@ -431,7 +431,7 @@ STEP_OPS = ("symp", "symh", "tw", "jfac", "vert", "b3", "bsd", "b2", "lap", "inv
             "kv", "kd", "ktt", "kq", "ww", "tmtx", "minv", "vdiff", "frc3", "frcs", "dft",
             "tc_anal", "tc_synth")
 STEP_DIMS = ("prec", "nmem", "nlat", "nlon", "nmax", "kmax", "nsets", "strictly_linear",
-             "vd_on0", "vd_on1", "vd_on2", "vd_on3", "frc_shared", "legendre")
+             "vd_on0", "vd_on1", "vd_on2", "vd_on3", "frc_shared", "legendre", "tc_off", "tc_g")
 
 _DESC_CACHE = {}
 
@@ -451,7 +451,7 @@ def _desc(state, work, ops, dims, consts):
     for i in range(4):
         d.vd_on[i] = dims[8 + i]
     d.frc_shared = dims[12]
-    d.legendre = dims[13]
+    d.legendre, d.tc_off, d.tc_g = dims[13], dims[14], dims[15]
     d.kappa, d.epsvt, d.robert = (float(x) for x in consts)
     for name, t in zip(STEP_OPS + STEP_WORK, list(ops) + list(work)):
         setattr(d, name, _p(t))

@@ -113,6 +113,9 @@ class EnsembleStepper:
         self.cd = torch.complex128 if precision == "fp64" else torch.complex64
         self.prec_id = _lib.LBM_F64 if precision == "fp64" else _lib.LBM_F32
         self.legendre = self.LEGENDRE[precision]
+        # tile choices of the tensor-core kernels (see tune()): which of the
+        # analysis / synthesis stay on the FMA kernels, members per MMA tile
+        self.tc_off, self.tc_g = 0, 0
         self.E = E = int(nmem)
         self.N = N = sp.nmax
         self.M = M = N + 1
@@ -334,7 +337,8 @@ class EnsembleStepper:
         names = {"vdiff": "vdm"}
         opsl = [z(getattr(self, names.get(n, n))) for n in _ops.STEP_OPS]
         dims = [self.prec_id, self.E, self.J, self.I, self.N, self.K, len(self._dts),
-                self.strictly_linear] + list(self.vd_on) + [self.frc_shared, self.legendre]
+                self.strictly_linear] + list(self.vd_on) + [self.frc_shared, self.legendre,
+                                                            self.tc_off, self.tc_g]
         consts = [KAPPA, EPSVT, self.robert]
         self.desc()
         self._oargs = (state, work, opsl, dims, consts)
@@ -344,6 +348,7 @@ class EnsembleStepper:
         if self._desc is not None:
             return self._desc
         self._oargs = None
+        self.desc_gen = getattr(self, "desc_gen", 0) + 1     # counts rebuilt descriptors
         d = StepperDesc()
         d.prec = self.prec_id
         d.nmem, d.nlat, d.nlon, d.nmax, d.kmax = self.E, self.J, self.I, self.N, self.K
@@ -367,6 +372,7 @@ class EnsembleStepper:
         d.legendre = self.legendre
         d.tc_anal = ptr(self.tc_anal)
         d.tc_synth = ptr(self.tc_synth)
+        d.tc_off, d.tc_g = self.tc_off, self.tc_g
         self._desc = d
         return d
 
