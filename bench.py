@@ -58,13 +58,14 @@ def parse():
                     help="skip the accuracy / plain-FP64 / CPU side measurements")
     ap.add_argument("--adjoint", action="store_true",
                     help="checkpointed-adjoint cost and accuracy (T42L20, 20 days, FP64, "
-                         "32 stored states) instead of the bench")
+                         "every state stored; 32 on the binomial schedule for comparison) "
+                         "instead of the bench")
     ap.add_argument("--adjoint-steps", type=int, default=None,
                     help="--adjoint over this many steps instead of 20 days (profiling)")
     ap.add_argument("--adjoint-members", type=int, default=None,
                     help="--adjoint: time one gradient of this many members (own heatings) "
                          "against one single-member gradient instead")
-    ap.add_argument("--fd-dirs", type=int, default=4,
+    ap.add_argument("--fd-dirs", type=int, default=16,
                     help="central-difference directions checked by --adjoint")
     ap.add_argument("--conditioning", action="store_true",
                     help="conditioning of the 30-day problem: FP64 against FP64 with every "
@@ -461,11 +462,14 @@ def conditioning(torch, days=(10, 30)):
     return out
 
 
-def adjoint_measurement(torch, days=20.0, snaps=32, fd_dirs=4, nsteps=None):
+def adjoint_measurement(torch, days=20.0, snaps=None, fd_dirs=16, nsteps=None,
+                        binomial_snaps=32):
     """Gradient of the area-mean day-20 streamfunction at sigma 0.25 over
     30-60N 150-210E with respect to the 20 x 64 x 128 heating (solid-body
     basic state, elliptic heating, plain damping, T42L20, FP64), by the
-    checkpointed adjoint; its time against the forward run of the same step
+    checkpointed adjoint (every call's state stored when they fit in half
+    the free device memory; also timed with ``binomial_snaps`` states on the
+    binomial schedule); its time against the forward run of the same step
     (graph-replayed reference-layout calls) and against the fused FP64
     stepper's run, and central differences (eps 1e-4 relative) along seeded
     directions."""
@@ -500,6 +504,10 @@ def adjoint_measurement(torch, days=20.0, snaps=32, fd_dirs=4, nsteps=None):
     seq = ForcingGradient(model, resp, ndays=days, snaps=snaps, pipeline=False)
     seq._fg, seq._ag = warm._fg, warm._ag
     (_, grad_seq), t_seq = timed(lambda: seq.value_and_grad(heat))
+    del seq
+    bino = ForcingGradient(model, resp, ndays=days, snaps=binomial_snaps)
+    bino._fg, bino._ag = warm._fg, warm._ag
+    (_, grad_bino), t_bino = timed(lambda: bino.value_and_grad(heat))
     sf = _t.SimpleNamespace(t=heat, vor=None, div=None, ps=None)
     m2 = mk(1.0, precision="fp64")
     m2.run(steady_forcing=sf, verbose=False)          # warm-up (graph capture)
@@ -523,19 +531,25 @@ def adjoint_measurement(torch, days=20.0, snaps=32, fd_dirs=4, nsteps=None):
                     "FP64, 20 days (1440 steps + 2 start-up calls); response: area-mean psi' "
                     "at sigma 0.25, 30-60N x 150-210E, day 20",
         "J": float(J), "J_forward_run": float(J_fwd), "J_fused_fp64_run": J_fused,
-        "snaps": snaps, "peak_stored_states": fg.peak_stored, "calls": calls,
+        "snaps": fg.snaps, "peak_stored_states": fg.peak_stored, "calls": calls,
+        "stored_state_bytes": fg.state_bytes(),
         "forward_steps_in_gradient": fg.forward_steps,
         "forward_s": t_fwd, "gradient_s": t_grad, "gradient_over_forward": t_grad / t_fwd,
         "gradient_one_stream_s": t_seq,
         "one_stream_vs_two_max_rel_diff": float((grad_seq - grad).abs().max()
                                                 / grad.abs().max()),
         "fused_fp64_forward_s": t_fused, "gradient_over_fused_forward": t_grad / t_fused,
+        "binomial": {"snaps": binomial_snaps, "forward_steps_in_gradient": bino.forward_steps,
+                     "gradient_s": t_bino, "gradient_over_forward": t_bino / t_fwd,
+                     "gradient_over_fused_forward": t_bino / t_fused,
+                     "max_rel_diff_vs_all_stored": float((grad_bino - grad).abs().max()
+                                                         / grad.abs().max())},
         "fd_rel_err": fd, "fd_max_rel_err": max(fd) if fd else None,
         "grad_absmax": float(grad.abs().max()),
     }
 
 
-def adjoint_batched_measurement(torch, nmem, nsteps, snaps=32):
+def adjoint_batched_measurement(torch, nmem, nsteps, snaps=None):
     """One gradient of ``nmem`` members (seeded ensemble heatings, T42L20,
     FP64, each member its own response) reversed together, against one
     single-member gradient over the same calls."""
@@ -548,7 +562,7 @@ def adjoint_batched_measurement(torch, nmem, nsteps, snaps=32):
     heats = torch.as_tensor(configs.ensemble_heating(128, 64, sigm, nmem, seed=SEED)[0],
                             device="cuda")
     cfg = lambda: Config(**configs.plain_damping(K))   # noqa: E731
-    out = {"members": nmem, "calls": nsteps + 2, "snaps": snaps}
+    out = {"members": nmem, "calls": nsteps + 2}
     runs = (("single", None), ("batched", nmem))
     for name, E in runs:
         if E is None:
@@ -563,6 +577,7 @@ def adjoint_batched_measurement(torch, nmem, nsteps, snaps=32):
         warm.value_and_grad(h)
         fg = ForcingGradient(m, resp, nsteps=nsteps, snaps=snaps)
         fg._fg, fg._ag = warm._fg, warm._ag
+        out[f"{name}_snaps"] = fg.snaps
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         J, g = fg.value_and_grad(h)

@@ -449,13 +449,18 @@ class ForcingGradient:
     """J(heating) and dJ/d(heating) for a steady 3-D heating (K/s, the
     ``frc_t`` argument of every call), from the model's zero initial state,
     over the calls of ``LBM._schedule(nsteps)`` (start-up calls included).
-    The reverse sweep re-advances from at most ``snaps`` stored states.
-    With ``use_graph`` every forward call and every adjoint call replays a
+    The reverse sweep re-advances from at most ``snaps`` stored states;
+    ``snaps=None`` stores every call's state when they fit in ``mem_frac`` of
+    the device memory free at construction (no re-steps: one forward sweep,
+    then the adjoint calls), else as many as fit, up to ``MAX_SNAPS``, on the
+    binomial schedule.  With ``use_graph`` every forward call and every adjoint call replays a
     CUDA graph of its (dt, start-up) variant; the kernels and their order
     are those of the eager calls, so the results are bitwise the same."""
 
-    def __init__(self, model, response, nsteps=None, ndays=None, snaps=32, use_graph=True,
-                 pipeline=True):
+    MAX_SNAPS = 256          # the binomial recursion's depth grows with the states
+
+    def __init__(self, model, response, nsteps=None, ndays=None, snaps=None, use_graph=True,
+                 pipeline=True, mem_frac=0.5):
         self.step = TimeStep(model)
         self.use_graph = bool(use_graph)
         self.pipeline = bool(pipeline)
@@ -465,11 +470,31 @@ class ForcingGradient:
             nsteps = int(round((ndays if ndays is not None else model.cfg.ndays)
                                * model.cfg.steps_per_day))
         self.calls = model._schedule(nsteps)
+        if snaps is None:
+            snaps = self.auto_snaps(len(self.calls), self.state_bytes(), mem_frac)
         self.snaps = int(snaps)
         self.actions = binomial_schedule(len(self.calls), self.snaps)
         self.forward_steps = 0
         self.peak_stored = 0
         self._saved = None
+
+    def state_bytes(self):
+        """Device bytes of one stored (ga, gb) pair."""
+        st = self.step
+        cols = st.nmem * st.sp.nlat * st.sp.nlon
+        return 2 * cols * (4 * st.vg.kmax + 1) * 8
+
+    @classmethod
+    def auto_snaps(cls, ncalls, pair_bytes, mem_frac=0.5, free_bytes=None):
+        """Stored states for ``ncalls`` calls: all of them (plus the one the
+        last call makes) when they fit in ``mem_frac`` of ``free_bytes``
+        (default: the device's free memory), else as many as fit, capped."""
+        if free_bytes is None:
+            free_bytes = torch.cuda.mem_get_info()[0]
+        fit = int(mem_frac * free_bytes) // max(1, pair_bytes)
+        if fit >= ncalls + 1:
+            return ncalls
+        return max(1, min(fit, cls.MAX_SNAPS))
 
     def _heating(self, heating):
         sp, vg = self.step.sp, self.step.vg

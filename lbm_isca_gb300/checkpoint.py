@@ -67,6 +67,17 @@ def schedule(nsteps, snaps):
     if nsteps < 1 or snaps < 1:
         raise ValueError("need nsteps >= 1 and snaps >= 1")
     out = [("store", 0)]
+    if snaps >= nsteps:
+        # every state fits: one forward sweep storing each, then the adjoints
+        # in reverse order, each state dropped once reversed (t - 1 steps,
+        # the bound at c >= t)
+        for i in range(nsteps - 1):
+            out += [("advance", i, i + 1), ("store", i + 1)]
+        for i in range(nsteps - 1, -1, -1):
+            out += [("restore", i), ("adjoint", i)]
+            if i:
+                out.append(("free", i))
+        return out
     cache = {}
 
     def split(t, c):

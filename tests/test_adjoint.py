@@ -53,6 +53,10 @@ def test_binomial_schedule_meets_the_bound():
     # 20 days at dt = 1200 s (1440 steps + 2 start-up calls), 32 stored states
     steps, peak, order = simulate(schedule(1442, 32))
     assert peak == 32 and len(order) == 1442 and steps == binomial_cost(1442, 32) == 3731
+    # every state stored: one forward sweep, no re-step
+    steps, peak, order = simulate(schedule(1442, 1442))
+    assert (steps, peak) == (1441, 1442) == (binomial_cost(1442, 1442), 1442)
+    assert order == list(range(1441, -1, -1))
     with pytest.raises(ValueError):
         schedule(0, 3)
     with pytest.raises(ValueError):
@@ -118,6 +122,18 @@ class _ToyStep:
         return pa, pb, dt * ac.u
 
 
+def test_auto_stored_states():
+    """Every call's state when the trajectory fits the memory share, else as
+    many as fit, capped; never fewer than one."""
+    pytest.importorskip("torch")
+    from lbm_isca_gb300.adjoint import ForcingGradient as FG
+    pair = 2 * 64 * 128 * (4 * 20 + 1) * 8           # one T42L20 member, FP64
+    assert FG.auto_snaps(1442, pair, 0.5, free_bytes=200 << 30) == 1442
+    assert FG.auto_snaps(1442, pair, 0.5, free_bytes=8 << 30) == FG.MAX_SNAPS
+    assert FG.auto_snaps(1442, pair, 0.5, free_bytes=100 * pair) == 50
+    assert FG.auto_snaps(1442, pair, 0.5, free_bytes=0) == 1
+
+
 def test_gradient_driver_bookkeeping_on_a_toy_model():
     """The checkpointed gradient of a toy model equals central differences
     and the every-state-stored gradient, for several stored-state counts."""
@@ -148,7 +164,7 @@ def test_gradient_driver_bookkeeping_on_a_toy_model():
 
     h = torch.as_tensor(np.random.default_rng(8).normal(size=shape))
     ref = None
-    for snaps in (1, 2, 3, 5, 40):
+    for snaps in (1, 2, 3, 5, 15, 40):
         fg = driver(snaps)
         J, g = fg.value_and_grad(h)
         assert fg.peak_stored <= snaps
