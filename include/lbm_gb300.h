@@ -279,11 +279,19 @@ int lbm_implicit_step_adjoint(int prec, const lbm_implicit_adj_args* a, void* st
  *        n (zero for n = 0; rows past N are zero), each as three bfloat16
  *        pieces, each piece a JT x 16 tile (rows = latitudes of the part,
  *        K = kk) in the layout of tc_anal
- *   tc_off: with legendre != 0, bit 0 keeps the analysis and bit 1 the
- *        synthesis on the FMA kernels (0 = both on the tensor cores)
+ *   tc_off: with legendre != 0, bit 0 keeps the Legendre analysis, bit 1
+ *        the Legendre synthesis and bit 2 the longitude analysis on the FMA
+ *        kernels (0 = all on the tensor cores where supported)
  *   tc_g: at most this many members per 128-lane MMA tile of the tensor-core
  *        kernels (0 = as many as fit, 128 / (2 kmax)); fewer members make
  *        more, smaller units of work (a choice of the tile autotuner)
+ *   tc_dft: table image of the tensor-core longitude analysis (legendre != 0
+ *        with nlon <= 128, 2 (nmax + 1) <= 128 and 2 + 9 kmax <= 256;
+ *        NULL otherwise), 16-byte aligned: for each step s of 16 longitudes,
+ *        three bfloat16 pieces (split from FP64 as for tc_anal) of the
+ *        128 x 16 tile W[L][i] = cos(2 pi m (16 s + i) / nlon) / nlon for
+ *        L = 2m and -sin(...) / nlon for L = 2m + 1 (zero for m > nmax), in
+ *        the layout of tc_anal
  * sf, af and grid9 must be 16-byte aligned (LBM_ERR_ARG otherwise).
  * ==========================================================================*/
 enum {
@@ -310,6 +318,7 @@ typedef struct lbm_stepper_desc {
   const void* tc_synth;
   int tc_off;
   int tc_g;
+  const void* tc_dft;
 } lbm_stepper_desc;
 
 /* Per-step control.  dt: time step of this call; set: which operator set

@@ -79,7 +79,7 @@ class StepperDesc(C.Structure):
                                      "tends", "grid6", "grid9")]
                 + [("err", C.POINTER(I32)), ("err_member", C.POINTER(I32)),
                    ("legendre", I32), ("tc_anal", VP), ("tc_synth", VP), ("tc_off", I32),
-                   ("tc_g", I32)])
+                   ("tc_g", I32), ("tc_dft", VP)])
 
 
 class StepCtl(C.Structure):

@@ -1,12 +1,13 @@
 """Tile autotuner of the tensor-core Legendre kernels.
 
 For a stepper in a tensor-core precision ("bf16x3", "bf16split") the
-choices are, per transform direction, the tensor-core kernel or the FP32 FMA
-kernel (both FP32-level in bf16x3), and the members per 128-lane MMA tile
+choices are, per contraction (Legendre analysis, Legendre synthesis,
+longitude analysis), the tensor-core kernel or the FP32 FMA kernel (both
+FP32-level in bf16x3), and the members per 128-lane MMA tile
 (the tile's M extent: (members, level, Re|Im) rows; fewer members give more,
 smaller units of work, which pays for small ensembles).  On first use of a
-(GPU, grid, levels, members, precision) each candidate's analysis and
-synthesis launches are timed with CUDA events on the stepper's stream and the
+(GPU, grid, levels, members, precision) each candidate's three launches
+are timed with CUDA events on the stepper's stream and the
 fastest is kept in a JSON cache (``$LBM_AUTOTUNE_CACHE``, by default
 ``lbm_isca_gb300/_lib/autotune.json`` next to the library); later steppers of
 the same shape read the choice from it.
@@ -34,13 +35,18 @@ def _key(stp):
 
 
 def candidates(stp):
-    """(tc_off, tc_g) pairs: tc_off bit 0 = analysis on FMA, bit 1 =
-    synthesis on FMA; tc_g = members per MMA tile (0 = as many as fit)."""
+    """(tc_off, tc_g) pairs: tc_off bit 0 = Legendre analysis on FMA, bit 1 =
+    Legendre synthesis on FMA, bit 2 = longitude analysis on FMA (only where
+    its tensor-core form exists); tc_g = members per MMA tile (0 = as many as
+    fit; it does not change the longitude analysis)."""
     gmax = max(1, min(128 // (2 * stp.K), stp.E))
     gs = sorted({gmax, max(1, gmax // 2), 1}, reverse=True)
-    out = [(3, 0)]
-    for off in (0, 1, 2):
-        out += [(off, g) for g in gs]
+    dft = (0, 4) if stp.tc_dft is not None else (4,)
+    out = []
+    for b2 in dft:
+        out.append((3 | b2, 0))
+        for off in (0, 1, 2):
+            out += [(off | b2, g) for g in gs]
     return out
 
 
@@ -51,7 +57,8 @@ def _apply(stp, off, g):
 
 
 def time_choice(stp, off, g, reps=5, warm=2):
-    """ms of one analysis + one synthesis launch with the given choice."""
+    """ms of one Legendre analysis, one Legendre synthesis and one longitude
+    analysis launch with the given choice."""
     _apply(stp, off, g)
     ctl = (StepCtl * 1)()
     ctl[0].dt, ctl[0].set, ctl[0].ps_mode, ctl[0].ra_mode = stp._dts[0], 0, 0, 1
@@ -60,13 +67,13 @@ def time_choice(stp, off, g, reps=5, warm=2):
     d = stp.desc()
     with torch.cuda.stream(stp.stream):
         for _ in range(warm):
-            for kern in (1, 3):
+            for kern in (1, 3, 6):
                 check(L.lbm_stepper_launch(C.byref(d), ctl, kern, s), "lbm_stepper_launch")
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stp.stream)
         for _ in range(reps):
-            for kern in (1, 3):
+            for kern in (1, 3, 6):
                 check(L.lbm_stepper_launch(C.byref(d), ctl, kern, s), "lbm_stepper_launch")
         e1.record(stp.stream)
     stp.stream.synchronize()

@@ -53,8 +53,10 @@ template <typename R> struct SD {
   int legendre;                          // 0 FMA; 3 or 6: tensor-core products
   const unsigned char* tc_anal;          // table image of k_anal_tc
   const unsigned char* tc_synth;         // table image of k_synth_tc
-  int tc_off;                            // bit 0: analysis, bit 1: synthesis on FMA
+  int tc_off;                            // bits 0 / 1 / 2: Legendre analysis / synthesis,
+                                         // longitude analysis on FMA
   int tc_g;                              // members per MMA tile cap (0: as many as fit)
+  const unsigned char* tc_dft;           // table image of k_fdft_tc
 };
 
 template <typename R> SD<R> make_sd(const lbm_stepper_desc& d) {
@@ -85,6 +87,7 @@ template <typename R> SD<R> make_sd(const lbm_stepper_desc& d) {
   s.tc_synth = (const unsigned char*)d.tc_synth;
   s.tc_off = d.tc_off;
   s.tc_g = d.tc_g;
+  s.tc_dft = (const unsigned char*)d.tc_dft;
   return s;
 }
 
@@ -1039,6 +1042,7 @@ __global__ void k_ps_flush(SD<R> d, int ps_mode) {
 #include "grid_split.cuh"
 #include "legendre_tc.cuh"
 #include "synth_tc.cuh"
+#include "dft_tc.cuh"
 namespace lbm {
 
 // ---- launch configuration ------------------------------------------------------
@@ -1162,7 +1166,12 @@ template <typename R, int I> int launch_step(const SD<R>& d, const lbm_step_ctl&
       k_idft<I><<<dim3(d.J, d.E), IDFT_NT, idft_smem(I, d.M), st>>>(d, d.dft);
     if (only < 0 || only == 0 || only == 5)
       k_alg<I><<<dim3(d.J, d.E), I, 0, st>>>(d, c.ps_mode);
-    if (only < 0 || only == 0 || only == 6) {
+    if ((only < 0 || only == 0 || only == 6) && d.legendre && !(d.tc_off & 4) &&
+        ftc_supported(I, d.K, d.N)) {
+      const FtcPlan pl = ftc_plan(d.E, d.J, I, d.K, d.N);
+      k_fdft_tc<<<persistent_grid((const void*)k_fdft_tc, FTC_THREADS, pl.smem, pl.nunits),
+                  FTC_THREADS, pl.smem, st>>>(d, d.tc_dft, pl, d.legendre);
+    } else if (only < 0 || only == 0 || only == 6) {
       const FdftPlan pl = fdft_plan(I, d.M, d.K);
       const size_t smem = sizeof(float) * (size_t)pl.total;
       const int nunits = d.E * d.J * ((d.K + pl.lc - 1) / pl.lc);
@@ -1202,6 +1211,11 @@ template <typename R, int I> void set_attrs(const SD<R>& d) {
     if (smem <= 227 * 1024) {
       cudaFuncSetAttribute(k_fdft<I>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       persistent_grid((const void*)k_fdft<I>, pl.nt, smem, 1);
+    }
+    if (d.legendre && ftc_supported(I, d.K, d.N)) {
+      const FtcPlan fp = ftc_plan(d.E, d.J, I, d.K, d.N);
+      cudaFuncSetAttribute(k_fdft_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fp.smem);
+      persistent_grid((const void*)k_fdft_tc, FTC_THREADS, fp.smem, 1);
     }
   } else {
     cudaFuncSetAttribute(k_grid<R, I, KB, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1254,8 +1268,11 @@ template <typename R> int validate(const SD<R>& d) {
         !d.tc_synth || (d.J % 16) || (d.K & 1) || d.M > 256 ||
         atc_plan(d.E, d.J, d.K, d.N, d.tc_g).smem > 227 * 1024 ||
         stc_plan(d.E, d.J, d.K, d.N, d.tc_g).smem > 227 * 1024 ||
-        (stc_plan(d.E, d.J, d.K, d.N).JT % 16) || d.tc_off < 0 || d.tc_off > 3 ||
+        (stc_plan(d.E, d.J, d.K, d.N).JT % 16) || d.tc_off < 0 || d.tc_off > 7 ||
         d.tc_g < 0 ||
+        (ftc_supported(d.I, d.K, d.N) &&
+         (!d.tc_dft || ((uintptr_t)d.tc_dft & 15) ||
+          ftc_plan(d.E, d.J, d.I, d.K, d.N).smem > 227 * 1024)) ||
         ((uintptr_t)d.tc_anal & 15) || ((uintptr_t)d.tc_synth & 15))
       return LBM_ERR_ARG;
   }

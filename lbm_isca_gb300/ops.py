@@ -429,7 +429,7 @@ STEP_STATE = ("sa3", "sas", "sb3", "psa", "psb", "err", "err_member")
 STEP_WORK = ("sf", "sfs", "af", "afs", "tend", "tends", "grid6", "grid9")
 STEP_OPS = ("symp", "symh", "tw", "jfac", "vert", "b3", "bsd", "b2", "lap", "invlap", "nn1a",
             "kv", "kd", "ktt", "kq", "ww", "tmtx", "minv", "vdiff", "frc3", "frcs", "dft",
-            "tc_anal", "tc_synth")
+            "tc_anal", "tc_synth", "tc_dft")
 STEP_DIMS = ("prec", "nmem", "nlat", "nlon", "nmax", "kmax", "nsets", "strictly_linear",
              "vd_on0", "vd_on1", "vd_on2", "vd_on3", "frc_shared", "legendre", "tc_off", "tc_g")
 

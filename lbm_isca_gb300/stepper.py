@@ -95,6 +95,30 @@ def tc_synth_image(P, H, invlap, N):
     return torch.cat(out).contiguous()
 
 
+def tc_dft_image(N, I, device="cpu"):
+    """Table image of the tensor-core longitude analysis (the tc_dft layout
+    of include/lbm_gb300.h): per step of 16 longitudes, the 128 x 16 tile
+    W[2m][i] = cos(2 pi m i / I) / I, W[2m + 1][i] = -sin(2 pi m i / I) / I
+    (zero rows for m > N), split from FP64 into three bfloat16 pieces, each
+    a K-major tile of 8-row x 16-byte core matrices.  Returns int16 words."""
+    KS = I // 16
+    m = torch.arange(64, dtype=torch.float64, device=device)
+    i = torch.arange(I, dtype=torch.float64, device=device)
+    ang = (2.0 * np.pi / I) * torch.remainder(m[:, None] * i[None, :], I)
+    W = torch.zeros((128, I), dtype=torch.float64, device=device)
+    W[0::2] = torch.cos(ang) / I
+    W[1::2] = -torch.sin(ang) / I
+    W[2 * (N + 1):] = 0.0
+    pieces, r = [], W
+    for _ in range(3):
+        b = r.to(torch.bfloat16)
+        pieces.append(b.view(torch.int16))
+        r = r - b.to(torch.float64)
+    x = torch.stack(pieces, 0)                            # [p][128][I]
+    x = x.reshape(3, 16, 8, KS, 2, 8)                     # [p][rg][r8][s][kc][k8]
+    return x.permute(3, 0, 1, 4, 2, 5).reshape(-1).contiguous()
+
+
 class EnsembleStepper:
     """Fused GPU time stepping of `nmem` members sharing one basic state."""
 
@@ -189,6 +213,10 @@ class EnsembleStepper:
         self.tc_anal = self._tc_anal_image() if self.legendre else None
         self.tc_synth = (tc_synth_image(sp.pnm, sp.hnm, sp.inv_laplace, N)
                          if self.legendre else None)
+        # the longitude analysis on the tensor cores where its plan applies
+        # (nlon <= 128, 2 + 9 kmax <= 256 rows)
+        self.tc_dft = (tc_dft_image(N, I, dev) if self.legendre and I <= 128
+                       and 2 + 9 * K <= 256 else None)
         # FP32 grid rows between the longitude transforms and the column algebra
         if precision != "fp64":
             f = lambda *s_: torch.zeros(s_, device=dev, dtype=torch.float32)   # noqa: E731
@@ -372,6 +400,7 @@ class EnsembleStepper:
         d.legendre = self.legendre
         d.tc_anal = ptr(self.tc_anal)
         d.tc_synth = ptr(self.tc_synth)
+        d.tc_dft = ptr(self.tc_dft)
         d.tc_off, d.tc_g = self.tc_off, self.tc_g
         self._desc = d
         return d

@@ -95,6 +95,73 @@ def test_analysis_kernel_vs_fp64(torch, case):
     assert errs["bf16split"] < 1e-3, errs
 
 
+def _oracle_longitude_analysis(g9, jfac, M):
+    """af [E][M][J][K][7] and afs [E][M][J][2] of the grid rows g9
+    [E][J][2 + 9K][I] in FP64: X = rfft / I of each row, then per level
+    (rows gt xu g yu fu fv ke xv yv) FU = wd X(fu), FV = wd X(fv),
+    KE = wg X(ke), T = wg X(gt) - wd i m X(xu), XV = wd X(xv),
+    Q = wg X(g) - wd i m X(yu), YV = wd X(yv); surface rows wg X."""
+    E, J, R, I = g9.shape
+    K = (R - 2) // 9
+    X = np.fft.rfft(g9, axis=-1)[..., :M] / I              # [E][J][R][M]
+    wg, wd = jfac[0][None, :, None, None], jfac[1][None, :, None, None]
+    lev = X[:, :, 2:].reshape(E, J, K, 9, M)               # [E][J][K][f][M]
+    im = 1j * np.arange(M)
+    f = lambda i: lev[:, :, :, i]                           # noqa: E731  [E][J][K][M]
+    fields = [wd * f(4), wd * f(5), wg * f(6), wg * f(0) - wd * im * f(1),
+              wd * f(7), wg * f(2) - wd * im * f(3), wd * f(8)]
+    af = np.stack(fields, -1).transpose(0, 3, 1, 2, 4)     # [E][M][J][K][7]
+    afs = (wg * X[:, :, :2]).transpose(0, 3, 1, 2)         # [E][M][J][2]
+    return af, afs
+
+
+@pytest.mark.parametrize("case", ["T21L20", "T42L20"])
+def test_longitude_analysis_kernel_vs_fp64(torch, case):
+    """Kernel 6 (grid rows -> af, afs): the FMA k_fdft in fp32 and the
+    tensor-core k_fdft_tc in bf16x3 / bf16split against the FP64 rfft."""
+    from lbm_isca_gb300._lib import StepCtl, check, lib
+    from lbm_isca_gb300.backend import stream_handle
+    nlon, nlat, nmax, K, E = CASES[case]
+    M = nmax + 1
+    rng = np.random.default_rng(23)
+    g9 = rng.normal(size=(E, nlat, 2 + 9 * K, nlon)).astype(np.float32)
+    got = {}
+    ref = None
+    for prec in ("fp32", "bf16x3", "bf16split"):
+        stp = _stepper(torch, case, prec)
+        if prec != "fp32":
+            assert stp.tc_dft is not None
+            stp.tc_off = 0
+            stp._desc = stp._oargs = None
+        if ref is None:
+            jfac = stp.jfac.double().cpu().numpy()
+            ref = _oracle_longitude_analysis(g9.astype(np.float64), jfac, M)
+        stp.grid9.copy_(torch.as_tensor(g9, device="cuda"))
+        stp.af.zero_()
+        stp.afs.zero_()
+        ctl = (StepCtl * 1)()
+        ctl[0].dt, ctl[0].set, ctl[0].ps_mode, ctl[0].ra_mode = 1200.0, 0, 0, 1
+        with torch.cuda.stream(stp.stream):
+            check(lib().lbm_stepper_launch(C.byref(stp.desc()), ctl, 6,
+                                           stream_handle(stp.stream)), "longitude analysis")
+        stp.stream.synchronize()
+        assert int(stp.err.item()) == 0
+        got[prec] = (stp.af.cpu().numpy().astype(np.complex128),
+                     stp.afs.cpu().numpy().astype(np.complex128))
+    err = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))   # noqa: E731
+    errs = {p: (err(a, ref[0]), err(b, ref[1])) for p, (a, b) in got.items()}
+    e32 = max(errs["fp32"])
+    assert e32 < 2e-6, errs
+    assert max(errs["bf16x3"]) < max(2e-6, 3 * e32), errs
+    assert max(errs["bf16split"]) < 1e-3, errs
+
+
+def test_longitude_analysis_t85_stays_on_fma(torch):
+    """nlon = 256 is past the tensor-core plan: no table, the FMA kernel runs."""
+    stp = _stepper(torch, "T85L40", "bf16x3")
+    assert stp.tc_dft is None
+
+
 def _oracle_synthesis(tr, sa3, K):
     """sf [E][M][J][K][6] of the packed state sa3 [E][4][NS][K] in FP64:
     U = i m P il div - H il vor, V = i m P il vor + H il div, then P vor,

@@ -248,3 +248,27 @@ def test_tensor_core_synthesis_table_image_layout():
                     assert abs(val - ref) <= 2.0 ** -24 * abs(ref) + 1e-36, (m, part, s, t, r)
             base += nparts * ks * 12 * JT * 16
         assert base == img.size
+
+
+def test_tensor_core_longitude_table_image_layout():
+    """The tc_dft table image: per 16-longitude step three bfloat16 pieces of
+    the 128 x 16 tile W[2m][i] = cos(2 pi m i / I) / I, W[2m+1][i] =
+    -sin(2 pi m i / I) / I (zero past nmax), each element at the byte the
+    header gives, pieces summing to the FP64 value to 2^-24."""
+    from lbm_isca_gb300.stepper import tc_dft_image
+    for (I, N) in ((64, 21), (128, 42)):
+        img = tc_dft_image(N, I).numpy().view(np.uint16)
+        KS = I // 16
+        assert img.size == KS * 3 * 128 * 16
+
+        def bf16(u):
+            return (u.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+        for s in range(KS):
+            for L in range(128):
+                for kk in range(16):
+                    m, c, i = L // 2, L % 2, 16 * s + kk
+                    ang = 2.0 * np.pi * ((m * i) % I) / I
+                    ref = 0.0 if m > N else (np.cos(ang) if c == 0 else -np.sin(ang)) / I
+                    off = (L // 8) * 128 + (kk // 8) * 64 + (L % 8) * 8 + kk % 8
+                    val = sum(bf16(img[(s * 3 + p) * 2048 + off]) for p in range(3))
+                    assert abs(val - ref) <= 2.0 ** -24 * abs(ref) + 1e-36, (I, s, L, kk)
