@@ -39,9 +39,23 @@ K_LEV = 20
 SEED = 1
 DTYPES = {"fp32": "f32", "fp64": "f64", "bf16x3": "bf16x3 split, f32 accumulate",
           "bf16split": "bf16x2 split, f32 accumulate"}
-LEGENDRE_NOTE = {"fp32": "on the FP32 FMA pipes", "fp64": "in FP64",
-                 "bf16x3": "on the tensor cores (tcgen05, bf16 3-way split, 6 products)",
-                 "bf16split": "on the tensor cores (tcgen05, bf16 2-way split, 3 products)"}
+SPLIT_NOTE = {"bf16x3": "tcgen05, bf16 3-way split, 6 products, FP32 accumulate",
+              "bf16split": "tcgen05, bf16 2-way split, 3 products, FP32 accumulate"}
+
+
+def placement(stp):
+    """Where the step's contractions run, from the stepper's own choice."""
+    if stp.precision == "fp64":
+        return "all contractions in FP64"
+    if not stp.legendre:
+        return "all contractions on the FP32 FMA pipes"
+    on = {"Legendre analysis": not (stp.tc_off & 1), "Legendre synthesis": not (stp.tc_off & 2),
+          "longitude analysis of the level rows": (stp.tc_dft is not None
+                                                   and not (stp.tc_off & 4))}
+    tc = [k for k, v in on.items() if v]
+    fma = [k for k, v in on.items() if not v] + ["longitude synthesis", "surface rows"]
+    return (f"{', '.join(tc) or 'nothing'} on the tensor cores ({SPLIT_NOTE[stp.precision]}); "
+            f"{', '.join(fma)} on the FP32 FMA pipes")
 
 
 def parse():
@@ -51,8 +65,12 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--members", type=int, default=512)
-    ap.add_argument("--precision", default="fp32",
+    ap.add_argument("--precision", default="bf16x3",
                     choices=["fp32", "fp64", "bf16x3", "bf16split"])
+    ap.add_argument("--tc-off", type=int, default=-1,
+                    help="bf16 modes: contractions kept on the FMA pipes (bit 0 Legendre "
+                         "analysis, 1 Legendre synthesis, 2 longitude analysis; -1: the "
+                         "precision's default)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the accuracy / plain-FP64 / CPU side measurements")
@@ -60,6 +78,8 @@ def parse():
                     help="checkpointed-adjoint cost and accuracy (T42L20, 20 days, FP64, "
                          "every state stored; 32 on the binomial schedule for comparison) "
                          "instead of the bench")
+    ap.add_argument("--adjoint-precision", default="fp64", choices=["fp64", "fp32"],
+                    help="--adjoint: working precision of the adjoint and its forward runs")
     ap.add_argument("--adjoint-steps", type=int, default=None,
                     help="--adjoint over this many steps instead of 20 days (profiling)")
     ap.add_argument("--adjoint-members", type=int, default=None,
@@ -229,7 +249,8 @@ def build_model(E, precision, torch, days=1.0, seed=SEED, device="cuda"):
     nlon, nlat, nmax = GRID
     sigm = configs.equal_sigma_half_levels(K_LEV)
     bs = configs.solid_body_basic_state(nlon, nlat, sigm)
-    cfg = Config(ndays=days, precision=precision, **configs.plain_damping(K_LEV))
+    cfg = Config(ndays=days, precision=precision, tc_off=TC_OFF,
+                 **configs.plain_damping(K_LEV))
     model, spb, vg = make_ensemble_model(bs, E, cfg, device=device, nlon=nlon, nlat=nlat,
                                          nmax=nmax, sigm=sigm)
     heats, _ = configs.ensemble_heating(nlon, nlat, sigm, E, seed=seed)
@@ -290,6 +311,14 @@ def algorithmic_bytes(E, p):
     else:
         out["grid"] = E * (sf + af + 4 * p * J * I) + shared_grid
     return out
+
+
+def traffic_key(stp, name):
+    """Record name of a step kernel in the traffic file: `name`, or
+    `name`_tc when that contraction runs on the tensor cores."""
+    tc = stp.legendre and {"anal": not (stp.tc_off & 1), "synth": not (stp.tc_off & 2),
+                           "fdft": stp.tc_dft is not None and not (stp.tc_off & 4)}.get(name)
+    return name + "_tc" if tc else name
 
 
 def read_traffic(kernel, E):
@@ -463,7 +492,7 @@ def conditioning(torch, days=(10, 30)):
 
 
 def adjoint_measurement(torch, days=20.0, snaps=None, fd_dirs=16, nsteps=None,
-                        binomial_snaps=32):
+                        binomial_snaps=32, precision="fp64"):
     """Gradient of the area-mean day-20 streamfunction at sigma 0.25 over
     30-60N 150-210E with respect to the 20 x 64 x 128 heating (solid-body
     basic state, elliptic heating, plain damping, T42L20, FP64), by the
@@ -472,7 +501,10 @@ def adjoint_measurement(torch, days=20.0, snaps=None, fd_dirs=16, nsteps=None,
     binomial schedule); its time against the forward run of the same step
     (graph-replayed reference-layout calls) and against the fused FP64
     stepper's run, and central differences (eps 1e-4 relative) along seeded
-    directions."""
+    directions.  With ``precision="fp32"`` the adjoint, its forward run and
+    the fused forward run are FP32, and the gradient is compared with the
+    FP64 one instead of central differences (FP32 rounding swamps a
+    1e-4 difference quotient)."""
     import types as _t
     from lbm_isca_gb300 import LBM, Config, Spectral, VerticalGrid, configs
     from lbm_isca_gb300.adjoint import AreaMeanStreamfunction, ForcingGradient
@@ -484,13 +516,21 @@ def adjoint_measurement(torch, days=20.0, snaps=None, fd_dirs=16, nsteps=None,
     mk = lambda nd, **kw: LBM(bs, sp, vg, Config(ndays=nd, **dict(configs.plain_damping(K),  # noqa
                                                                    **kw)))
     model = mk(days)
-    resp = AreaMeanStreamfunction(sp, vg)
-    warm = ForcingGradient(model, resp, nsteps=4, snaps=2)
+    resp64 = AreaMeanStreamfunction(sp, vg)
+
+    def gradient(n=None, **kw):
+        g = ForcingGradient(model, None, precision=precision, **(kw if n is None else
+                                                                  dict(kw, nsteps=n)))
+        g.response = resp64 if precision == "fp64" else AreaMeanStreamfunction(g.step.sp, vg)
+        return g
+
+    warm = gradient(4, snaps=2)
     warm.value_and_grad(heat)                        # captures every graph variant
     if nsteps is not None:
         days = nsteps / model.cfg.steps_per_day
-    fg = ForcingGradient(model, resp, ndays=days, snaps=snaps)
+    fg = gradient(ndays=days, snaps=snaps)
     fg._fg, fg._ag = warm._fg, warm._ag
+    resp = fg.response
 
     def timed(fn):
         torch.cuda.synchronize()
@@ -501,21 +541,34 @@ def adjoint_measurement(torch, days=20.0, snaps=None, fd_dirs=16, nsteps=None,
 
     J_fwd, t_fwd = timed(lambda: fg.value(heat))
     (J, grad), t_grad = timed(lambda: fg.value_and_grad(heat))
-    seq = ForcingGradient(model, resp, ndays=days, snaps=snaps, pipeline=False)
+    seq = gradient(ndays=days, snaps=snaps, pipeline=False)
     seq._fg, seq._ag = warm._fg, warm._ag
     (_, grad_seq), t_seq = timed(lambda: seq.value_and_grad(heat))
     del seq
-    bino = ForcingGradient(model, resp, ndays=days, snaps=binomial_snaps)
+    bino = gradient(ndays=days, snaps=binomial_snaps)
     bino._fg, bino._ag = warm._fg, warm._ag
     (_, grad_bino), t_bino = timed(lambda: bino.value_and_grad(heat))
+    bino_steps = bino.forward_steps
+    del bino
     sf = _t.SimpleNamespace(t=heat, vor=None, div=None, ps=None)
-    m2 = mk(1.0, precision="fp64")
+    m2 = mk(1.0, precision=precision)
     m2.run(steady_forcing=sf, verbose=False)          # warm-up (graph capture)
     m2.cfg.ndays = days
     _, t_fused = timed(lambda: m2.run(steady_forcing=sf, verbose=False))
-    m3 = mk(days, precision="fp64")
+    m3 = mk(days, precision=precision)
     m3.run(steady_forcing=sf, verbose=False)
-    J_fused = float(resp(m3.ga))
+    J_fused = float(resp64(m3.ga))
+    vs64 = None
+    if precision != "fp64":
+        fd_dirs = 0
+        g64 = ForcingGradient(model, resp64, ndays=days)
+        J64, grad64 = g64.value_and_grad(heat)
+        del g64
+        vs64 = {"J_rel_diff": abs(float(J) - float(J64)) / abs(float(J64)),
+                "grad_max_rel_diff": float((grad.double() - grad64).abs().max()
+                                           / grad64.abs().max()),
+                "grad_l2_rel_diff": float(torch.linalg.norm(grad.double() - grad64)
+                                          / torch.linalg.norm(grad64))}
     rng = np.random.default_rng(16)
     hmax = float(heat.abs().max())
     fd = []
@@ -528,9 +581,10 @@ def adjoint_measurement(torch, days=20.0, snaps=None, fd_dirs=16, nsteps=None,
     calls = len(fg.calls)
     return {
         "workload": "T42L20 solid-body basic state, elliptic heating (0N 120E), plain damping, "
-                    "FP64, 20 days (1440 steps + 2 start-up calls); response: area-mean psi' "
-                    "at sigma 0.25, 30-60N x 150-210E, day 20",
-        "J": float(J), "J_forward_run": float(J_fwd), "J_fused_fp64_run": J_fused,
+                    f"{precision.upper()}, 20 days (1440 steps + 2 start-up calls); response: "
+                    "area-mean psi' at sigma 0.25, 30-60N x 150-210E, day 20",
+        "precision": precision,
+        "J": float(J), "J_forward_run": float(J_fwd), "J_fused_run": J_fused,
         "snaps": fg.snaps, "peak_stored_states": fg.peak_stored, "calls": calls,
         "stored_state_bytes": fg.state_bytes(),
         "forward_steps_in_gradient": fg.forward_steps,
@@ -538,13 +592,14 @@ def adjoint_measurement(torch, days=20.0, snaps=None, fd_dirs=16, nsteps=None,
         "gradient_one_stream_s": t_seq,
         "one_stream_vs_two_max_rel_diff": float((grad_seq - grad).abs().max()
                                                 / grad.abs().max()),
-        "fused_fp64_forward_s": t_fused, "gradient_over_fused_forward": t_grad / t_fused,
-        "binomial": {"snaps": binomial_snaps, "forward_steps_in_gradient": bino.forward_steps,
+        "fused_forward_s": t_fused, "gradient_over_fused_forward": t_grad / t_fused,
+        "binomial": {"snaps": binomial_snaps, "forward_steps_in_gradient": bino_steps,
                      "gradient_s": t_bino, "gradient_over_forward": t_bino / t_fwd,
                      "gradient_over_fused_forward": t_bino / t_fused,
                      "max_rel_diff_vs_all_stored": float((grad_bino - grad).abs().max()
                                                          / grad.abs().max())},
         "fd_rel_err": fd, "fd_max_rel_err": max(fd) if fd else None,
+        "vs_fp64_gradient": vs64,
         "grad_absmax": float(grad.abs().max()),
     }
 
@@ -592,8 +647,13 @@ def adjoint_batched_measurement(torch, nmem, nsteps, snaps=None):
     return out
 
 
+TC_OFF = -1
+
+
 def main():
+    global TC_OFF
     args = parse()
+    TC_OFF = args.tc_off
     if args.adjoint and args.adjoint_members:
         import torch
         torch.cuda.set_device(0)
@@ -604,7 +664,8 @@ def main():
     if args.adjoint:
         import torch
         torch.cuda.set_device(0)
-        out = adjoint_measurement(torch, fd_dirs=args.fd_dirs, nsteps=args.adjoint_steps)
+        out = adjoint_measurement(torch, fd_dirs=args.fd_dirs, nsteps=args.adjoint_steps,
+                                  precision=args.adjoint_precision)
         print(json.dumps({"adjoint": out}), flush=True)
         return
     if args.config4:
@@ -755,8 +816,7 @@ def main():
             "dtype": DTYPES[args.precision], "data": "synthetic",
             "config": {"workload": f"{E}-member T42L20 ensemble (solid-body basic state, "
                                    f"seeded elliptic heatings seed {SEED}+rank, plain "
-                                   f"damping), FP32 state, fused stepper, Legendre analysis "
-                                   f"{LEGENDRE_NOTE[args.precision]}",
+                                   f"damping), FP32 state, fused stepper; {placement(stp)}",
                        "members_per_gpu": E, "grid": "T42 128x64 Gaussian",
                        "levels": "L20 equal sigma", "dt_s": delt,
                        "l2": "inputs larger than L2 (per-step working set "
@@ -764,10 +824,10 @@ def main():
                        "parallelism": f"members sharded, {world} independent rank(s)"},
             "clocks": clk.summary(),
             "e2e": e2e,
-            "gpu_launches": (nk + (1 if stp.legendre else 0)) * args.steps,
+            "gpu_launches": stp.launches_per_step() * args.steps,
             "roofline": {"bound": "hbm", "kernel": names[top], "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": read_traffic(names[top], E),
+                         "traffic": read_traffic(traffic_key(stp, names[top]), E),
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
             "roofline_step": step_roofline(E, p, t_max / args.steps, peaks, args.precision),
             "kernel_ms": dict(zip(names, [float(x) for x in kern_ms])),

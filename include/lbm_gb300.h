@@ -285,13 +285,15 @@ int lbm_implicit_step_adjoint(int prec, const lbm_implicit_adj_args* a, void* st
  *   tc_g: at most this many members per 128-lane MMA tile of the tensor-core
  *        kernels (0 = as many as fit, 128 / (2 kmax)); fewer members make
  *        more, smaller units of work (a choice of the tile autotuner)
- *   tc_dft: table image of the tensor-core longitude analysis (legendre != 0
- *        with nlon <= 128, 2 (nmax + 1) <= 128 and 2 + 9 kmax <= 256;
- *        NULL otherwise), 16-byte aligned: for each step s of 16 longitudes,
- *        three bfloat16 pieces (split from FP64 as for tc_anal) of the
- *        128 x 16 tile W[L][i] = cos(2 pi m (16 s + i) / nlon) / nlon for
- *        L = 2m and -sin(...) / nlon for L = 2m + 1 (zero for m > nmax), in
- *        the layout of tc_anal
+ *   tc_dft: table image of the longitude analysis of the level rows on the
+ *        tensor cores (legendre != 0 with nlon <= 128 a power of two and
+ *        9 kmax <= 256; NULL otherwise), 16-byte aligned: for each step s of
+ *        16 longitudes, three bfloat16 pieces (split from FP64 as for
+ *        tc_anal) of the 128 x 16 tile W[L][i] = cos(2 pi m (16 s + i) /
+ *        nlon) / nlon for L = 2m and -sin(...) / nlon for L = 2m + 1 (zero
+ *        for m > nmax), in the layout of tc_anal; then nlon FP32 values
+ *        cos(2 pi t / nlon), t = 0..nlon-1, the table of the two surface
+ *        rows, which stay on the FMA pipes
  * sf, af and grid9 must be 16-byte aligned (LBM_ERR_ARG otherwise).
  * ==========================================================================*/
 enum {

@@ -45,6 +45,7 @@ from .backend import to_device
 from .checkpoint import schedule as binomial_schedule
 from .configs import response_box
 from .constants import EPSVT, KAPPA, RAIR
+from .dynamics import Dynamics
 from .state import State
 
 FIELDS = ("u", "v", "t", "q", "ps")
@@ -85,24 +86,25 @@ class AdjointTransforms:
     spectral coefficients."""
 
     def __init__(self, sp):
-        if sp.precision != "fp64":
-            raise ValueError("the adjoint runs in FP64")
+        if sp.precision not in ("fp64", "fp32"):
+            raise ValueError("the adjoint runs in FP64 or FP32")
         self.sp = sp
         M, I = sp.nmax + 1, sp.nlon
-        dev = sp.device
+        dev, rd = sp.device, sp.rdtype
         cm = torch.full((M,), 2.0 * I, dtype=torch.float64, device=dev)
         cm[0] = float(I)
         hm = torch.full((M,), 0.5 / I, dtype=torch.float64, device=dev)
         hm[0] = 1.0 / I
-        t = sp._t
-        self.Pc = (t["P"] * cm[:, None, None]).contiguous()
-        self.Hc = (t["H"] * cm[:, None, None]).contiguous()
-        self.Pgw_h = (t["Pgw"] * hm[:, None, None]).contiguous()
-        self.Pgwdel_h = (t["Pgwdel"] * hm[:, None, None]).contiguous()
-        self.Hgwdel_h = (t["Hgwdel"] * hm[:, None, None]).contiguous()
-        self.neg_one = -torch.ones(M, dtype=torch.float64, device=dev)
-        self.neg_invlap = (-t["invlap"]).contiguous()
-        self.neg_cos = (-t["cos"]).contiguous()
+        # rescaled from the FP64 tables, rounded once to the working precision
+        sc = lambda T, f: (T * f[:, None, None]).to(rd).contiguous()   # noqa: E731
+        self.Pc = sc(sp.pnm, cm)
+        self.Hc = sc(sp.hnm, cm)
+        self.Pgw_h = sc(sp.pnm_gw, hm)
+        self.Pgwdel_h = sc(sp.pnm_gwdel, hm)
+        self.Hgwdel_h = sc(sp.hnm_gwdel, hm)
+        self.neg_one = -torch.ones(M, dtype=rd, device=dev)
+        self.neg_invlap = (-sp.inv_laplace).to(rd).contiguous()
+        self.neg_cos = (-sp.coslat).to(rd).contiguous()
 
     def wave_to_grid_T(self, g):
         sp = self.sp
@@ -155,20 +157,52 @@ class AdjointTransforms:
 # ---------------------------------------------------------------------------
 # The time step, its tangent-linear model and its adjoint
 # ---------------------------------------------------------------------------
-class TimeStep:
-    """One reference step on grid states of an ``LBM`` (FP64): one member,
-    or E members (a batched model, ``make_ensemble_model``) whose states
-    carry a leading member axis and advance together; members share the
-    basic state and operators and are otherwise independent."""
+VG_FIELDS = ("dsig", "sigm", "alpha", "w3", "wP", "cpg", "sig", "ww", "tmtx", "tbar", "gg")
+BS_FIELDS = ("u", "v", "t", "q", "tv", "absvor", "div", "x5", "sdot", "pix", "piy", "ps")
 
-    def __init__(self, model):
+
+def _cast(obj, names, dtype, **extra):
+    """A namespace of ``obj``'s named device arrays rounded to ``dtype``."""
+    return types.SimpleNamespace(**{n: getattr(obj, n).to(dtype).contiguous() for n in names},
+                                 **extra)
+
+
+class TimeStep:
+    """One reference step on grid states of an ``LBM``: one member, or E
+    members (a batched model, ``make_ensemble_model``) whose states carry a
+    leading member axis and advance together; members share the basic state
+    and operators and are otherwise independent.
+
+    ``precision="fp64"`` runs on the model's own FP64 objects.  ``"fp32"``
+    runs the same kernels in FP32 (every C entry point of the step and its
+    adjoint has an FP32 form): the transform tables come from an FP32
+    ``Spectral`` of the same grid, and the vertical operators, basic state
+    and semi-implicit / vertical-diffusion inverses are the model's FP64
+    arrays rounded once."""
+
+    def __init__(self, model, precision="fp64"):
+        if precision not in ("fp64", "fp32"):
+            raise ValueError("precision must be 'fp64' or 'fp32'")
         self.m = model
+        self.precision = precision
         self.nmem = model.nmem if model.batched else 1
         self.nd = 4 if model.batched else 3     # dimensions of a level-carrying field
-        self.sp, self.vg = model.sp, model.vg
-        self.tr = AdjointTransforms(model.sp)
-        self.ps_bar = model.ga.ps_bar
-        self.lnps_bar = model.ga.lnps_bar
+        self.rd = torch.float64 if precision == "fp64" else torch.float32
+        self.cd = torch.complex128 if precision == "fp64" else torch.complex64
+        sp = model.sp
+        if precision == "fp64":
+            self.sp, self.vg, self.bs, self.dyn = sp, model.vg, model.bst, model.dyn
+        else:
+            self.sp = type(sp)(nlon=sp.nlon, nlat=sp.nlat, nmax=sp.nmax, radius=sp.a,
+                               device=sp.device, precision="fp32")
+            self.vg = _cast(model.vg, VG_FIELDS, self.rd, kmax=model.vg.kmax,
+                            device=model.vg.device)
+            self.bs = _cast(model.bst, BS_FIELDS, self.rd)
+            self.dyn = Dynamics(self.sp, self.vg, self.bs, model.dyn.strictly_linear)
+        self._iops = {}
+        self.tr = AdjointTransforms(self.sp)
+        self.ps_bar = model.ga.ps_bar.to(self.rd)
+        self.lnps_bar = model.ga.lnps_bar.to(self.rd)
         self.gamma = float(model.cfg.robert)
         self.linear = bool(model.cfg.strictly_linear)
 
@@ -180,9 +214,9 @@ class TimeStep:
         attribute later (a second LBM on the same VerticalGrid resets its
         reference-temperature operators)."""
         m = self.m
-        objs = [self.sp, self.sp._t, self.vg, m.bst, m.damping, m.integ.semi,
+        objs = [self.sp, self.sp._t, self.vg, self.bs, m.bst, m.damping, m.integ.semi,
                 m.integ.semi._cache, m.integ.vdiff.minv, m.integ.vdiff._cache, self.tr,
-                {"ps_bar": self.ps_bar, "lnps_bar": self.lnps_bar}]
+                self._iops, {"ps_bar": self.ps_bar, "lnps_bar": self.lnps_bar}]
         out, seen = [], set()
 
         def grab(x, depth):
@@ -210,9 +244,51 @@ class TimeStep:
 
     def zero_state(self):
         J, I, K = self.sp.nlat, self.sp.nlon, self.vg.kmax
-        f64 = dict(dtype=torch.float64, device=self.sp.device)
-        z3 = lambda: torch.zeros(self._lead() + (J, I, K), **f64)   # noqa: E731
-        return self._state(z3(), z3(), z3(), z3(), torch.zeros(self._lead() + (J, I), **f64))
+        f = dict(dtype=self.rd, device=self.sp.device)
+        z3 = lambda: torch.zeros(self._lead() + (J, I, K), **f)   # noqa: E731
+        return self._state(z3(), z3(), z3(), z3(), torch.zeros(self._lead() + (J, I), **f))
+
+    def _pi(self, st):
+        """pi' of a grid state.  FP64 keeps the reference's ln(ps_bar + ps') -
+        ln(ps_bar) (state.py:77-79); FP32 takes log1p(ps' / ps_bar), the same
+        quantity without the cancellation of two logarithms near 11.5."""
+        if self.precision == "fp64":
+            return st.lnps_pert()
+        return torch.log1p(st.ps / self.ps_bar)
+
+    def _ps(self, pi):
+        """ps' = ps_bar (exp(pi') - 1) (state.py:81-83); expm1 in FP32."""
+        if self.precision == "fp64":
+            return self.ps_bar * (torch.exp(pi) - 1.0)
+        return self.ps_bar * torch.expm1(pi)
+
+    def implicit_ops(self, dt):
+        """The operator list of ``implicit_step`` / ``implicit_step_adjoint``
+        for a time step, in the working precision (IMPL_OPS order)."""
+        integ, vg = self.m.integ, self.m.vg
+        integ.semi.prepare(dt)
+        integ.vdiff.prepare(dt)
+        dmp = integ.dmp
+        mv = integ.vdiff.minv
+        opsl = [self.m.sp.laplace, dmp.kv, dmp.kd, dmp.ktt, dmp.kq, vg.ww, vg.tmtx, vg.gg,
+                vg.dsig, integ.semi.minv] + [mv.get(n) for n in ("vor", "div", "t", "q")]
+        if self.precision == "fp64":
+            return opsl
+        key = float(dt)
+        if key not in self._iops:
+            self._iops[key] = [None if x is None else x.to(self.rd).contiguous() for x in opsl]
+        return self._iops[key]
+
+    def _istep(self, dt, prev, tend):
+        """Integrator.step in the working precision."""
+        if self.precision == "fp64":
+            return self.m.integ.step(dt, prev, tend)
+        keys = ("vor", "div", "t", "pi", "q")
+        c = lambda x: x.to(self.cd).contiguous()     # noqa: E731
+        new = torch.ops.lbm_gb300.implicit_step(
+            self.implicit_ops(dt), [c(prev[k]) for k in keys], [c(x) for x in tend],
+            self.nmem, self.sp.nmax, self.vg.kmax, float(dt))
+        return dict(zip(keys, new))
 
     def _ra(self, prev, cur, nxt):
         g = self.gamma
@@ -227,11 +303,11 @@ class TimeStep:
         that share a call made in one launch over concatenated columns."""
         m, sp, K, nd = self.m, self.sp, self.vg.kmax, self.nd
         vo, di = sp.uv_to_vordiv(_cat([ga.u, gb.u], nd), _cat([ga.v, gb.v], nd))
-        s = sp.grid_to_wave(_cat([ga.lnps_pert(), gb.t, gb.q, gb.lnps_pert()], nd))
+        s = sp.grid_to_wave(_cat([self._pi(ga), gb.t, gb.q, self._pi(gb)], nd))
         g = sp.wave_to_grid(_cat([vo[..., :K], di[..., :K]], nd))
         pix, piy = sp.hgrad(s[..., 0])
-        o = m.dyn._grid_kernel(ga, g[..., :K], g[..., K:], pix, piy, frc_t, None, None,
-                               want_omega=False)
+        o = self.dyn._grid_kernel(ga, g[..., :K], g[..., K:], pix, piy, frc_t, None, None,
+                                  want_omega=False)
         w = sp.grid_to_wave(_cat([o["gt_pi"], o["gt"], o["ke"], o["g"]], nd))
         fvo, fdi = sp.uv_to_vordiv(_cat([o["fu"], o["xu"], o["yu"]], nd),
                                    _cat([o["fv"], o["xv"], o["yv"]], nd))
@@ -240,11 +316,11 @@ class TimeStep:
                 -fdi[..., 2 * K:] + w[..., 2 * K + 1:])
         prev = {"vor": vo[..., K:], "div": di[..., K:], "t": s[..., 1:K + 1],
                 "pi": s[..., 2 * K + 1], "q": s[..., K + 1:2 * K + 1]}
-        new = m.integ.step(dt, prev, tend)
+        new = self._istep(dt, prev, tend)
         u, v = sp.vordiv_to_uv(new["vor"], new["div"])
         gg = sp.wave_to_grid(_cat([new["t"], new["q"], new["pi"]], nd))
         gc = self._state(u, v, gg[..., :K], gg[..., K:2 * K],
-                         self.ps_bar * (torch.exp(gg[..., 2 * K]) - 1.0))
+                         self._ps(gg[..., 2 * K]))
         gb_new = ga if start else self._ra(gb, ga, gc)
         return gc, gb_new
 
@@ -268,8 +344,8 @@ class TimeStep:
         dpi = dga.ps / (self.ps_bar + ga.ps)
         pix, piy = sp.hgrad(sp.grid_to_wave(dpi))
         lin = None if self.linear else (ga.u, ga.v)
-        o = self.m.dyn._grid_kernel(dga, vor, div, pix, piy, dfrc, None, None,
-                                    want_omega=False, lin=lin)
+        o = self.dyn._grid_kernel(dga, vor, div, pix, piy, dfrc, None, None,
+                                  want_omega=False, lin=lin)
         return self._assemble(o)
 
     def tangent(self, ga, gb, gc_ps, dga, dgb, dt, start, dfrc=None):
@@ -281,7 +357,7 @@ class TimeStep:
         prev = {"vor": vor, "div": div, "t": sp.grid_to_wave(dgb.t),
                 "pi": sp.grid_to_wave(dgb.ps / (self.ps_bar + gb.ps)),
                 "q": sp.grid_to_wave(dgb.q)}
-        new = self.m.integ.step(dt, prev, tend)
+        new = self._istep(dt, prev, tend)
         u, v = sp.vordiv_to_uv(new["vor"], new["div"])
         dgc = self._state(u, v, sp.wave_to_grid(new["t"]), sp.wave_to_grid(new["q"]),
                           (self.ps_bar + gc_ps) * sp.wave_to_grid(new["pi"]))
@@ -290,7 +366,7 @@ class TimeStep:
 
     # ---- adjoint ------------------------------------------------------------
     def _tend_adjoint_kernel(self, ga, a_o):
-        sp, vg, bs = self.sp, self.vg, self.m.bst
+        sp, vg, bs = self.sp, self.vg, self.bs
         J, I, K = sp.nlat, sp.nlon, vg.kmax
         named = {"dsig": vg.dsig, "sigm": vg.sigm, "alpha": vg.alpha, "w3": vg.w3, "wP": vg.wP,
                  "cpg": vg.cpg, "ww": vg.ww, "tmtx": vg.tmtx, "tref": vg.tbar, "ub": bs.u,
@@ -299,7 +375,7 @@ class TimeStep:
                  "piyb": bs.piy, "u0": None if self.linear else ga.u,
                  "v0": None if self.linear else ga.v}
         for k in ("fu", "fv", "ke", "gt", "xu", "xv", "g", "yu", "yv", "gt_pi"):
-            named["a_" + k] = a_o[k].to(torch.float64)
+            named["a_" + k] = a_o[k].to(self.rd)
         outs = torch.ops.lbm_gb300.tendency_grid_adjoint(
             [named[k] for k in _ops.TADJ_INPUTS], self.nmem, J, I, K, [KAPPA, EPSVT, RAIR])
         return {k[2:]: t for k, t in zip(_ops.TADJ_OUTPUTS, outs)}
@@ -322,17 +398,10 @@ class TimeStep:
 
     def _implicit_adjoint(self, dt, an):
         sp, vg = self.sp, self.vg
-        integ = self.m.integ
-        integ.semi.prepare(dt)
-        integ.vdiff.prepare(dt)
-        dmp = integ.dmp
         keys = ("vor", "div", "t", "pi", "q")
-        mv = integ.vdiff.minv
-        opsl = [sp.laplace, dmp.kv, dmp.kd, dmp.ktt, dmp.kq, vg.ww, vg.tmtx, vg.gg, vg.dsig,
-                integ.semi.minv] + [mv.get(n) for n in ("vor", "div", "t", "q")]
         outs = torch.ops.lbm_gb300.implicit_step_adjoint(
-            opsl, [an[k].to(torch.complex128) for k in keys], self.nmem, sp.nmax, vg.kmax,
-            float(dt))
+            self.implicit_ops(dt), [an[k].to(self.cd) for k in keys], self.nmem, sp.nmax,
+            vg.kmax, float(dt))
         return dict(zip(keys, outs[:5])), dict(zip(keys, outs[5:]))
 
     def adjoint(self, ga, gb, gc_ps, a_ga, a_gb, dt, start):
@@ -460,8 +529,8 @@ class ForcingGradient:
     MAX_SNAPS = 256          # the binomial recursion's depth grows with the states
 
     def __init__(self, model, response, nsteps=None, ndays=None, snaps=None, use_graph=True,
-                 pipeline=True, mem_frac=0.5):
-        self.step = TimeStep(model)
+                 pipeline=True, mem_frac=0.5, precision="fp64"):
+        self.step = TimeStep(model, precision)
         self.use_graph = bool(use_graph)
         self.pipeline = bool(pipeline)
         self._fg, self._ag = {}, {}
@@ -482,7 +551,7 @@ class ForcingGradient:
         """Device bytes of one stored (ga, gb) pair."""
         st = self.step
         cols = st.nmem * st.sp.nlat * st.sp.nlon
-        return 2 * cols * (4 * st.vg.kmax + 1) * 8
+        return 2 * cols * (4 * st.vg.kmax + 1) * torch.empty(0, dtype=st.rd).element_size()
 
     @classmethod
     def auto_snaps(cls, ncalls, pair_bytes, mem_frac=0.5, free_bytes=None):
@@ -498,7 +567,7 @@ class ForcingGradient:
 
     def _heating(self, heating):
         sp, vg = self.step.sp, self.step.vg
-        h = to_device(heating, sp.device)
+        h = to_device(heating, sp.device).to(self.step.rd)
         want = self.step._lead() + (sp.nlat, sp.nlon, vg.kmax)
         if tuple(h.shape) != want:
             raise ValueError(f"heating must be ([nmem,] nlat, nlon, kmax) = {want}, "

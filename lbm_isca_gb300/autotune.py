@@ -34,19 +34,29 @@ def _key(stp):
     return (f"{name}|J{stp.J} I{stp.I} N{stp.N} K{stp.K} E{stp.E}|{stp.precision}")
 
 
+#: tc_off bits a precision must keep set (contractions that stay on the FMA
+#: pipes for accuracy): bf16x3 keeps the Legendre contractions there, since
+#: with them on the tensor cores (whose FP32 accumulation rounds toward zero)
+#: T42L20 exceeds the 1e-5 gate at day 30.
+FIXED = {"bf16x3": 3, "bf16split": 0}
+
+
 def candidates(stp):
     """(tc_off, tc_g) pairs: tc_off bit 0 = Legendre analysis on FMA, bit 1 =
     Legendre synthesis on FMA, bit 2 = longitude analysis on FMA (only where
     its tensor-core form exists); tc_g = members per MMA tile (0 = as many as
-    fit; it does not change the longitude analysis)."""
+    fit; it does not change the longitude analysis).  Choices that clear a
+    bit the precision keeps set (``FIXED``) are left out."""
     gmax = max(1, min(128 // (2 * stp.K), stp.E))
     gs = sorted({gmax, max(1, gmax // 2), 1}, reverse=True)
     dft = (0, 4) if stp.tc_dft is not None else (4,)
+    fixed = FIXED.get(stp.precision, 0)
     out = []
     for b2 in dft:
         out.append((3 | b2, 0))
         for off in (0, 1, 2):
-            out += [(off | b2, g) for g in gs]
+            if off & fixed == fixed:
+                out += [(off | b2, g) for g in gs]
     return out
 
 

@@ -1,8 +1,10 @@
-// Longitude analysis of the FP32 stepper (k_fdft's work: grid9 -> af, afs)
-// on the tensor cores, bfloat16 split operands, FP32 accumulation in TMEM.
+// Longitude analysis of the FP32 stepper (k_fdft's work: grid9 -> af, afs):
+// the 9K level rows on the tensor cores (k_fdft_tc: bfloat16 split operands,
+// FP32 accumulation in TMEM), the two surface rows on the FMA pipes
+// (k_fdft_surf).
 //
 // Per (member, latitude) unit the weighted Fourier coefficients of the R =
-// 2 + 9K grid rows are one product
+// 9K level rows are one product
 //   D[L][n] = sum_i W[L][i] G[n][i],  L = 2m + c,
 // with W[2m][i] = cos(2 pi m i / I) / I and W[2m+1][i] = -sin(2 pi m i / I) /
 // I (so D[2m] + i D[2m+1] is the rfft coefficient of row n over I, as
@@ -13,15 +15,25 @@
 // loads (the next unit pulled into L2 ahead) into a four-slot ring.  The
 // epilogue combines a level's rows as k_fdft does -- a3 = wg X(gt) -
 // wd i m X(xu), a5 = wg X(g) - wd i m X(yu), wd X(fu), wd X(fv), wg X(ke),
-// wd X(xv), wd X(yv), and wg X of the two surface rows -- with the i m
-// terms taken from the partner lane (L ^ 1), stages the unit's af rows in
-// shared memory and writes them as contiguous runs.
+// wd X(xv), wd X(yv) -- with the i m terms taken from the partner lane
+// (L ^ 1), stages the unit's af rows in shared memory and writes them as
+// contiguous runs.
 //
-// Roles (one persistent CTA per SM): warp 0 loads the table image once and
-// prefetches units into L2; warp 1 TMEM and MMA issue; warps 2..17 split
-// the grid rows; warps 18..21 the epilogue.  Bounded waits as in
+// Why the surface rows stay on FMA: the tensor cores' FP32 accumulation
+// rounds toward zero, so every coefficient comes out smaller in magnitude by
+// about 2.6e-7 relative (measured on GB300, T42: the FMA kernel's signed
+// error is 1e-9).  For tendencies that is noise, but the second surface row
+// is pi(t - dt), which goes spectral -> grid -> spectral every step (its
+// Robert-Asselin filter runs in grid space): the shrink would compound step
+// after step (the bf16x3 run then drifts to 4e-5 in pi at day 30).  The
+// Legendre tensor-core kernels keep the surface fields on FMA for the same
+// reason.
+//
+// Roles of k_fdft_tc (one persistent CTA per SM): warp 0 loads the table
+// image once and prefetches units into L2; warp 1 TMEM and MMA issue; warps
+// 2..17 split the grid rows; warps 18..21 the epilogue.  Bounded waits as in
 // legendre_tc.cuh.  Supported: nlon <= 128 (the table's 2 (nmax + 1) <= 128
-// lanes) and 2 + 9 kmax <= 256 rows.
+// lanes), nlon a power of two, and 9 kmax <= 256 rows.
 #pragma once
 #include "tc_common.cuh"
 #include "async_copy.cuh"
@@ -33,6 +45,11 @@ constexpr int FTC_CONV_WARPS = 16;
 constexpr int FTC_THREADS = 32 * (2 + FTC_CONV_WARPS + 4);
 constexpr int FTC_PREFETCH = 2;        // units of grid rows pulled into L2 ahead
 
+// Floats per wavenumber in the epilogue's staging area: the K x 7 complex of
+// a unit's af row plus 4, so that the 16 wavenumbers of a warp's stores fall
+// on 8 bank groups instead of 4 (the copy-out keeps 16-byte alignment).
+LBM_HD int ftc_stage_stride(int K) { return K * 14 + 4; }
+
 struct FtcPlan {
   int R, NR, KS, nunits, tcols;
   unsigned tab_bytes, b_bytes, out_bytes, smem;
@@ -40,7 +57,7 @@ struct FtcPlan {
 
 LBM_HD FtcPlan ftc_plan(int E, int J, int I, int K, int N) {
   FtcPlan p;
-  p.R = 2 + 9 * K;
+  p.R = 9 * K;
   p.NR = (p.R + 15) / 16 * 16;
   p.KS = I / 16;
   p.nunits = E * J;
@@ -48,14 +65,14 @@ LBM_HD FtcPlan ftc_plan(int E, int J, int I, int K, int N) {
   p.tcols = cols <= 128 ? 128 : cols <= 256 ? 256 : 512;
   p.tab_bytes = (unsigned)(p.KS * 3 * 4096);            // 128 lanes x 16 x 3 pieces per step
   p.b_bytes = (unsigned)(3 * p.NR * 32);
-  p.out_bytes = (unsigned)((N + 1) * K * 7 * 8);
+  p.out_bytes = (unsigned)((N + 1) * ftc_stage_stride(K) * 4);
   p.smem = 2048 + p.tab_bytes + FTC_BSLOTS * ((p.b_bytes + 1023) / 1024 * 1024) +
            (p.out_bytes + 1023) / 1024 * 1024;
   return p;
 }
 
 LBM_HD bool ftc_supported(int I, int K, int N) {
-  return I <= 128 && 2 * (N + 1) <= 128 && 2 + 9 * K <= 256 && (I % 16) == 0;
+  return I <= 128 && 2 * (N + 1) <= 128 && 9 * K <= 256 && (I % 16) == 0 && !(I & (I - 1));
 }
 
 struct FtcSmem {
@@ -63,11 +80,10 @@ struct FtcSmem {
   unsigned tslot;
 };
 
-// B row of grid row r: the level rows ordered (field, level) so that a
-// field's levels are adjacent columns of D; the two surface rows last.
-LBM_D int ftc_brow(int r, int K) {
-  if (r < 2) return 9 * K + r;
-  const int q = r - 2, k = q / 9, f = q - 9 * k;
+// B row of level row q (grid row 2 + q): ordered (field, level) so that a
+// field's levels are adjacent columns of D.
+LBM_D int ftc_brow(int q, int K) {
+  const int k = q / 9, f = q - 9 * k;
   return f * K + k;
 }
 
@@ -105,7 +121,7 @@ __global__ void __launch_bounds__(FTC_THREADS, 1)
   const unsigned tbase = sm->tslot;
   bool ok = true;
   const float* g9 = d.grid9;
-  const size_t unit_floats = (size_t)R * I;
+  const size_t unit_floats = (size_t)(2 + R) * I;      // a unit's grid rows, surface first
 
   if (warp == 0) {
     // ---------------- table once, then L2 prefetch of the units ahead ----------
@@ -160,8 +176,31 @@ __global__ void __launch_bounds__(FTC_THREADS, 1)
     }
   } else if (warp < 2 + FTC_CONV_WARPS) {
     // ---------------- conversion: grid rows -> B tiles ----------------
+    // One (B row, 8-longitude chunk) item per thread (2 NR <= 512 items):
+    // the 8 lanes of a quarter warp take 8 consecutive B rows of one chunk,
+    // so each 16-byte store of a quarter warp fills one 128-byte core-matrix
+    // row group (no bank conflicts).  The next step's rows are loaded into
+    // registers before this step's are split (the loads' latency is hidden
+    // behind the split and the wait for a free slot).
     const int ct = threadIdx.x - 64;
-    const int items = NR * 2;                    // (B row, 8-longitude chunk)
+    const int chk = (ct >> 3) & 1;
+    const int br = (ct & 7) | ((ct >> 4) << 3);  // B row (field f = br / K, level br % K)
+    const bool live = br < NR;                   // padding rows past R stay zero
+    const bool data = br < R;
+    const int q = 9 * (br % K) + br / K;         // its level row: ftc_brow(q, K) == br
+    const unsigned off = tile_offset(br, chk * 8);
+    auto load = [&](int u, int s, float4& x0, float4& x1) {
+      if (data && u < pl.nunits) {
+        const float4* src = reinterpret_cast<const float4*>(
+            g9 + (size_t)u * unit_floats + (size_t)(2 + q) * I + s * 16 + chk * 8);
+        x0 = __ldg(src);
+        x1 = __ldg(src + 1);
+      } else {
+        x0 = x1 = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    };
+    float4 n0, n1;
+    load(blockIdx.x, 0, n0, n1);
     unsigned a = 0;
     for (int u = blockIdx.x; u < pl.nunits && ok; u += gridDim.x) {
       if (ct == 0) {
@@ -169,46 +208,15 @@ __global__ void __launch_bounds__(FTC_THREADS, 1)
         if (un < pl.nunits)
           prefetch_l2_bulk(g9 + (size_t)un * unit_floats, (unsigned)(unit_floats * 4));
       }
-      const float* gu = g9 + (size_t)u * unit_floats;
       for (int s = 0; s < KS && ok; ++s, ++a) {
         const int slot = a % FTC_BSLOTS;
-        // the loads go out before the wait for a free slot
-        float4 v0[2], v1[2];
-        int brow[2], chk[2];
-        bool live[2];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int it = ct + h * 512;
-          live[h] = false;
-          brow[h] = 0;
-          chk[h] = 0;
-          v0[h] = v1[h] = make_float4(0.f, 0.f, 0.f, 0.f);
-          if (it < items) {
-            const int r = it >> 1;
-            chk[h] = it & 1;
-            live[h] = true;
-            if (r < R) {
-              brow[h] = ftc_brow(r, K);
-              const float4* src =
-                  reinterpret_cast<const float4*>(gu + (size_t)r * I + s * 16 + chk[h] * 8);
-              v0[h] = __ldg(src);
-              v1[h] = __ldg(src + 1);
-            } else {
-              brow[h] = r;                      // padding rows stay zero
-            }
-          }
-        }
+        const float x[8] = {n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, n1.z, n1.w};
+        if (s + 1 < KS) load(u, s + 1, n0, n1);
+        else load(u + gridDim.x, 0, n0, n1);
         ok = warp_wait(smem_addr(&sm->bempty[slot]), ((a / FTC_BSLOTS) & 1u) ^ 1u, err, ATC_ERR);
         if (!ok) break;
         unsigned char* bt = bring + slot * bslot;
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          if (!live[h]) continue;
-          const float x[8] = {v0[h].x, v0[h].y, v0[h].z, v0[h].w,
-                              v1[h].x, v1[h].y, v1[h].z, v1[h].w};
-          const unsigned off = tile_offset(brow[h], chk[h] * 8);
-          split3_store8(x, bt + off, bt + NR * 32 + off, bt + 2 * NR * 32 + off);
-        }
+        if (live) split3_store8(x, bt + off, bt + NR * 32 + off, bt + 2 * NR * 32 + off);
         fence_async_smem();
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_addr(&sm->bfull[slot]));
@@ -220,6 +228,7 @@ __global__ void __launch_bounds__(FTC_THREADS, 1)
     const int L = 32 * q4 + lane, m = L >> 1, c = L & 1;
     const bool live = m < M;
     const int et = threadIdx.x - 32 * (2 + FTC_CONV_WARPS);     // 0..127
+    const int SS = ftc_stage_stride(K);
     unsigned ul = 0;
     for (int u = blockIdx.x; u < pl.nunits && ok; u += gridDim.x, ++ul) {
       const int e = u / J, j = u - e * J;
@@ -277,7 +286,7 @@ __global__ void __launch_bounds__(FTC_THREADS, 1)
         const float pyu = __shfl_xor_sync(0xffffffffu, v[3], 1);
         const float sg = c ? -1.f : 1.f;        // Re: + wdm Im(xu); Im: - wdm Re(xu)
         if (live) {
-          float* o = stage + ((size_t)(m * K + k) * AF_N) * 2 + c;
+          float* o = stage + (size_t)m * SS + (k * AF_N) * 2 + c;
           o[2 * AF_T] = wg * v[0] + sg * wdm * pxu;
           o[2 * AF_Q] = wg * v[2] + sg * wdm * pyu;
           o[2 * AF_FU] = wd * v[4];
@@ -287,33 +296,19 @@ __global__ void __launch_bounds__(FTC_THREADS, 1)
           o[2 * AF_YV] = wd * v[8];
         }
       }
-      // surface rows: gt_pi and pi(t - dt)
-      {
-        unsigned r2[2];
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0, %1}, [%2];\n"
-            "tcgen05.wait::ld.sync.aligned;\n"
-            : "=r"(r2[0]), "=r"(r2[1])
-            : "r"(tl + (unsigned)(9 * K))
-            : "memory");
-        if (live) {
-          float* os = reinterpret_cast<float*>(d.afs) + ((((size_t)e * M + m) * J + j) * 2) * 2 + c;
-          os[0] = wg * __uint_as_float(r2[0]);
-          os[2] = wg * __uint_as_float(r2[1]);
-        }
-      }
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(smem_addr(&sm->accempty[b]));
       asm volatile("bar.sync 1, 128;\n" ::: "memory");
       // staged rows -> af: for each m, K * 7 complex contiguous
       const int rowf = K * AF_N * 2;                       // floats per m
-      const float4* s4 = reinterpret_cast<const float4*>(stage);
-      const int n4 = M * rowf / 4;
+      const int q4 = rowf / 4;                             // float4 per m
+      const int n4 = M * q4;
       float* afe = reinterpret_cast<float*>(d.af) + (((size_t)e * M) * J + j) * rowf;
       for (int x = et; x < n4; x += 128) {
-        const int mm = (x * 4) / rowf, w = x * 4 - mm * rowf;
-        *reinterpret_cast<float4*>(afe + (size_t)mm * J * rowf + w) = s4[x];
+        const int mm = x / q4, w = x - mm * q4;
+        *reinterpret_cast<float4*>(afe + (size_t)mm * J * rowf + 4 * w) =
+            *reinterpret_cast<const float4*>(stage + (size_t)mm * SS + 4 * w);
       }
     }
   }
@@ -323,6 +318,64 @@ __global__ void __launch_bounds__(FTC_THREADS, 1)
     __syncwarp();
     tc_fence_after();
     tmem_dealloc(tbase, (unsigned)pl.tcols);
+  }
+}
+
+// Surface rows (gt_pi, pi(t - dt)) of the longitude analysis on the FMA
+// pipes, rounded to nearest: one block per (latitude, FSURF_EB members), one
+// thread per lane L = 2m + c; W[L][i] read from an FP32 cos table (the sine
+// as cos(theta + pi / 2)), the members' rows staged [row][i][member] so that
+// a table value feeds 2 x FSURF_EB FMAs.  Writes afs = gw / I X, as k_fdft.
+constexpr int FSURF_EB = 8;
+
+inline size_t fsurf_smem(int I) { return sizeof(float) * (size_t)I * (1 + 2 * FSURF_EB); }
+
+__global__ void __launch_bounds__(128) k_fdft_surf(SD<float> d, const float* __restrict__ cs) {
+  extern __shared__ float4 sh_fsurf[];
+  float* tw = reinterpret_cast<float*>(sh_fsurf);
+  const int I = d.I, J = d.J, M = d.M, E = d.E, R = 2 + 9 * d.K;
+  float* rows = tw + I;                                  // [2][I][FSURF_EB]
+  const int j = blockIdx.x, e0 = blockIdx.y * FSURF_EB;
+  for (int t = threadIdx.x; t < I; t += blockDim.x) tw[t] = cs[t];
+  for (int x = threadIdx.x; x < 2 * I * FSURF_EB; x += blockDim.x) {
+    const int eb = x / (2 * I), rem = x - eb * 2 * I, r = rem / I, i = rem - r * I;
+    const int e = e0 + eb;
+    rows[(r * I + i) * FSURF_EB + eb] =
+        e < E ? d.grid9[(((size_t)e * J + j) * R + r) * I + i] : 0.f;
+  }
+  __syncthreads();
+  const int L = threadIdx.x, m = L >> 1, c = L & 1;
+  if (m >= M) return;
+  const int off = c ? I / 4 : 0;                         // -sin(t) = cos(t + pi / 2)
+  float acc[2][FSURF_EB];
+#pragma unroll
+  for (int h = 0; h < 2; ++h)
+#pragma unroll
+    for (int b = 0; b < FSURF_EB; ++b) acc[h][b] = 0.f;
+  for (int i = 0; i < I; ++i) {
+    const float w = tw[(m * i + off) & (I - 1)];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const float4* p = reinterpret_cast<const float4*>(rows + (size_t)(h * I + i) * FSURF_EB);
+#pragma unroll
+      for (int q = 0; q < FSURF_EB / 4; ++q) {
+        const float4 v = p[q];
+        acc[h][4 * q] = fmaf(w, v.x, acc[h][4 * q]);
+        acc[h][4 * q + 1] = fmaf(w, v.y, acc[h][4 * q + 1]);
+        acc[h][4 * q + 2] = fmaf(w, v.z, acc[h][4 * q + 2]);
+        acc[h][4 * q + 3] = fmaf(w, v.w, acc[h][4 * q + 3]);
+      }
+    }
+  }
+  const float wg = d.jfac[JF_GW * J + j] / float(I);
+#pragma unroll
+  for (int b = 0; b < FSURF_EB; ++b) {
+    const int e = e0 + b;
+    if (e < E) {
+      float* os = reinterpret_cast<float*>(d.afs) + ((((size_t)e * M + m) * J + j) * 2) * 2 + c;
+      os[0] = wg * acc[0][b];
+      os[2] = wg * acc[1][b];
+    }
   }
 }
 

@@ -1171,6 +1171,10 @@ template <typename R, int I> int launch_step(const SD<R>& d, const lbm_step_ctl&
       const FtcPlan pl = ftc_plan(d.E, d.J, I, d.K, d.N);
       k_fdft_tc<<<persistent_grid((const void*)k_fdft_tc, FTC_THREADS, pl.smem, pl.nunits),
                   FTC_THREADS, pl.smem, st>>>(d, d.tc_dft, pl, d.legendre);
+      // the surface rows on the FMA pipes; their FP32 cos table follows the
+      // tensor-core image
+      k_fdft_surf<<<dim3(d.J, (d.E + FSURF_EB - 1) / FSURF_EB), 128, fsurf_smem(I), st>>>(
+          d, reinterpret_cast<const float*>(d.tc_dft + pl.tab_bytes));
     } else if (only < 0 || only == 0 || only == 6) {
       const FdftPlan pl = fdft_plan(I, d.M, d.K);
       const size_t smem = sizeof(float) * (size_t)pl.total;

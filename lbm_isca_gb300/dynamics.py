@@ -101,7 +101,7 @@ class Dynamics:
         def frc(x, full_shape):
             if x is None:
                 return None, 0
-            t = to_device(x, dev)
+            t = to_device(x, dev, u.dtype)
             per = int(np.prod(full_shape[1:])) if batched else 0
             stride = per if (batched and t.dim() == len(full_shape)) else 0
             return t, stride

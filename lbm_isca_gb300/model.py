@@ -85,6 +85,9 @@ class Config:
                                   # precision of the step; the bf16 modes keep the FP32
                                   # state and run the Legendre analysis on the tensor
                                   # cores (3-way bf16 split, 6 or 3 products)
+    tc_off: int = -1              # bf16 modes: contractions kept on the FMA pipes (bit 0
+                                  # Legendre analysis, 1 synthesis, 2 longitude
+                                  # analysis); -1: the precision's default
     fused: bool = True            # fused ensemble stepper (False: general loop)
     use_graph: bool = True        # replay steady-state steps as CUDA graphs
     phase_timing: bool = False    # fused run: seconds per phase in LBM.phases
@@ -293,7 +296,8 @@ class LBM:
             self._stepper = EnsembleStepper(
                 self.sp, self.vg, self.bst, self.damping, self.semi, self.vdiff, self.nmem,
                 precision=self.cfg.precision, robert=self.cfg.robert,
-                strictly_linear=self.cfg.strictly_linear)
+                strictly_linear=self.cfg.strictly_linear,
+                tc_off=None if self.cfg.tc_off < 0 else self.cfg.tc_off)
         return self._stepper
 
     def _state_spectral(self, st):

@@ -302,6 +302,7 @@ def tendency_grid(ins: List[Optional[Tensor]], nmem: int, nlat: int, nlon: int, 
     Returns the TEND_OUTPUTS (omega has zero elements unless want_omega)."""
     keep = _Keep()
     u = ins[TEND_INPUTS.index("u")]
+    _same(_prec(u), *ins)
     s3, s2, ssd = _tend_shapes(ins, kmax)
     f = dict(device=u.device, dtype=u.dtype)
     outs = [torch.empty(s3, **f) for _ in range(9)] + [torch.empty(s2, **f)]
@@ -342,6 +343,7 @@ def implicit_step(ops: List[Optional[Tensor]], prev: List[Tensor], tend: List[Te
     (lbm_implicit_step): operators in IMPL_OPS order, previous level and
     explicit tendencies as (vor, div, t, pi, q); returns the new level."""
     keep = _Keep()
+    _same(_prec(prev[0]), *ops, *prev, *tend)
     out = [torch.empty_like(x) for x in prev]
     a = ImplicitArgs()
     a.nmem, a.nmax, a.kmax, a.dt = nmem, nmax, kmax, float(dt)
@@ -374,6 +376,7 @@ def tendency_grid_adjoint(ins: List[Optional[Tensor]], nmem: int, nlat: int, nlo
     TADJ_INPUTS order; returns TADJ_OUTPUTS."""
     keep = _Keep()
     afu = ins[TADJ_INPUTS.index("a_fu")]
+    _same(_prec(afu), *ins)
     s3 = tuple(afu.shape)
     outs = [torch.empty(s3, device=afu.device, dtype=afu.dtype) for _ in range(6)]
     outs += [torch.empty(s3[:-1], device=afu.device, dtype=afu.dtype) for _ in range(2)]
@@ -403,6 +406,7 @@ def implicit_step_adjoint(ops: List[Optional[Tensor]], an: List[Tensor], nmem: i
     the new level -> adjoints of the previous level and of the tendencies,
     (vor, div, t, pi, q) each."""
     keep = _Keep()
+    _same(_prec(an[0]), *ops, *an)
     ap = [torch.empty_like(x) for x in an]
     aw = [torch.empty_like(x) for x in an]
     a = ImplicitAdjArgs()

@@ -96,11 +96,13 @@ def tc_synth_image(P, H, invlap, N):
 
 
 def tc_dft_image(N, I, device="cpu"):
-    """Table image of the tensor-core longitude analysis (the tc_dft layout
-    of include/lbm_gb300.h): per step of 16 longitudes, the 128 x 16 tile
-    W[2m][i] = cos(2 pi m i / I) / I, W[2m + 1][i] = -sin(2 pi m i / I) / I
-    (zero rows for m > N), split from FP64 into three bfloat16 pieces, each
-    a K-major tile of 8-row x 16-byte core matrices.  Returns int16 words."""
+    """Table image of the longitude analysis on the tensor cores (the tc_dft
+    layout of include/lbm_gb300.h): per step of 16 longitudes, the 128 x 16
+    tile W[2m][i] = cos(2 pi m i / I) / I, W[2m + 1][i] = -sin(2 pi m i / I) /
+    I (zero rows for m > N), split from FP64 into three bfloat16 pieces, each
+    a K-major tile of 8-row x 16-byte core matrices; then the FP32 table
+    cos(2 pi t / I), t < I, of the surface rows' FMA kernel.  Returns int16
+    words."""
     KS = I // 16
     m = torch.arange(64, dtype=torch.float64, device=device)
     i = torch.arange(I, dtype=torch.float64, device=device)
@@ -116,17 +118,25 @@ def tc_dft_image(N, I, device="cpu"):
         r = r - b.to(torch.float64)
     x = torch.stack(pieces, 0)                            # [p][128][I]
     x = x.reshape(3, 16, 8, KS, 2, 8)                     # [p][rg][r8][s][kc][k8]
-    return x.permute(3, 0, 1, 4, 2, 5).reshape(-1).contiguous()
+    cs = torch.cos((2.0 * np.pi / I) * i).to(torch.float32).view(torch.int16)
+    return torch.cat([x.permute(3, 0, 1, 4, 2, 5).reshape(-1), cs]).contiguous()
 
 
 class EnsembleStepper:
     """Fused GPU time stepping of `nmem` members sharing one basic state."""
 
-    #: precision -> products of the tensor-core Legendre analysis (0: FMA pipes)
+    #: precision -> products of the tensor-core contractions (0: FMA pipes)
     LEGENDRE = {"fp64": 0, "fp32": 0, "bf16x3": 6, "bf16split": 3}
+    #: precision -> contractions kept on the FMA pipes by default (tc_off bits:
+    #: 0 Legendre analysis, 1 Legendre synthesis, 2 longitude analysis).  The
+    #: tensor cores' FP32 accumulation rounds toward zero; in bf16x3 only the
+    #: longitude analysis of the level rows goes to them by default, which
+    #: keeps the T42L20 day-30 error at 6.3e-6 (with the Legendre
+    #: contractions there too it reaches 1.1e-5, over the 1e-5 FP32 gate).
+    TC_OFF = {"bf16x3": 3, "bf16split": 0}
 
     def __init__(self, sp, vg, bst, damping, semi, vdiff, nmem, precision="fp64",
-                 robert=0.04, strictly_linear=False, stream=None):
+                 robert=0.04, strictly_linear=False, stream=None, tc_off=None):
         if precision not in self.LEGENDRE:
             raise ValueError(f"precision must be one of {sorted(self.LEGENDRE)}")
         self.sp, self.vg, self.bst = sp, vg, bst
@@ -139,7 +149,10 @@ class EnsembleStepper:
         self.legendre = self.LEGENDRE[precision]
         # tile choices of the tensor-core kernels (see tune()): which of the
         # analysis / synthesis stay on the FMA kernels, members per MMA tile
-        self.tc_off, self.tc_g = 0, 0
+        self.tc_off = int(self.TC_OFF.get(precision, 0) if tc_off is None else tc_off)
+        self.tc_g = 0
+        if not 0 <= self.tc_off <= 7:
+            raise ValueError("tc_off must be in 0..7")
         self.E = E = int(nmem)
         self.N = N = sp.nmax
         self.M = M = N + 1
@@ -213,10 +226,10 @@ class EnsembleStepper:
         self.tc_anal = self._tc_anal_image() if self.legendre else None
         self.tc_synth = (tc_synth_image(sp.pnm, sp.hnm, sp.inv_laplace, N)
                          if self.legendre else None)
-        # the longitude analysis on the tensor cores where its plan applies
-        # (nlon <= 128, 2 + 9 kmax <= 256 rows)
+        # the longitude analysis of the level rows on the tensor cores where
+        # its plan applies (nlon <= 128, 9 kmax <= 256 rows)
         self.tc_dft = (tc_dft_image(N, I, dev) if self.legendre and I <= 128
-                       and 2 + 9 * K <= 256 else None)
+                       and 9 * K <= 256 else None)
         # FP32 grid rows between the longitude transforms and the column algebra
         if precision != "fp64":
             f = lambda *s_: torch.zeros(s_, device=dev, dtype=torch.float32)   # noqa: E731
@@ -524,6 +537,20 @@ class EnsembleStepper:
         spec["pi"] = self.unpack(as_[:, 0], has_k=False)
         ps = self._hist["psa"][1].view(E, self.J, self.I) / n
         return spec, ps
+
+    def launches_per_step(self):
+        """Kernel launches of one step (lbm_stepper_run): FP64 k_grid,
+        k_anal, k_implicit, k_synth; FP32 k_idft, k_alg, k_fdft, k_anal,
+        k_implicit, k_synth, where each contraction on the tensor cores is
+        two launches (the tensor-core kernel and the surface fields' FMA
+        kernel)."""
+        if self.precision == "fp64":
+            return 4
+        n = 6
+        if self.legendre:
+            n += int(not (self.tc_off & 1)) + int(not (self.tc_off & 2))
+            n += int(self.tc_dft is not None and not (self.tc_off & 4))
+        return n
 
     def check_finite(self):
         """False when a member produced a non-finite value (bit 0 of err);

@@ -611,3 +611,45 @@ def test_batched_gradient_matches_single_members(torch_cuda):
     tl = fb.tangent(heats, d * float(heats.abs().max()))
     dots = (gb * d * float(heats.abs().max())).sum(dim=(1, 2, 3))
     assert float(((tl - dots).abs() / dots.abs()).max()) < 1e-10
+
+
+@pytest.mark.gpu
+def test_fp32_step_adjoint_dot_product(torch_cuda):
+    """The FP32 step: forward within 1e-4 (of each field's largest value) of
+    the FP64 step, and <TL dx, y> = <dx, ADJ y> to 1e-3 (start-up and
+    leapfrog calls)."""
+    from lbm_isca_gb300.adjoint import FIELDS, TimeStep, state_dot
+    m, _ = _model()
+    s64, s32 = TimeStep(m), TimeStep(m, "fp32")
+    r = _Rand(torch_cuda, 5)
+    f32 = lambda st: s32._state(*(getattr(st, k).float() for k in FIELDS))   # noqa: E731
+    ga, gb = r.state(s64, 5.0), r.state(s64, 5.0)
+    dga, dgb = r.state(s64), r.state(s64)
+    for start, dt in ((True, 300.0), (False, 1200.0)):
+        gc, gbn = s64.forward(ga, gb, dt, start, None)
+        gc32, gbn32 = s32.forward(f32(ga), f32(gb), dt, start, None)
+        for k in FIELDS:
+            for a, b in ((getattr(gc32, k), getattr(gc, k)), (getattr(gbn32, k), getattr(gbn, k))):
+                assert a.dtype == torch_cuda.float32
+                assert float((a.double() - b).abs().max()) <= 1e-4 * float(b.abs().max()), k
+        t1, t2 = s32.tangent(f32(ga), f32(gb), gc32.ps, f32(dga), f32(dgb), dt, start)
+        y1, y2 = f32(r.state(s64)), f32(r.state(s64))
+        lhs = state_dot(t1, y1) + state_dot(t2, y2)
+        a1, a2, _ = s32.adjoint(f32(ga), f32(gb), gc32.ps, y1, y2, dt, start)
+        assert all(getattr(a1, k).dtype == torch_cuda.float32 for k in FIELDS)
+        rhs = state_dot(f32(dga), a1) + state_dot(f32(dgb), a2)
+        assert _rel(lhs, rhs) < 1e-3, (lhs, rhs)
+
+
+@pytest.mark.gpu
+def test_fp32_gradient_against_fp64(gradient_case, torch_cuda):
+    """The FP32 checkpointed gradient over 36 calls against the FP64 one."""
+    from lbm_isca_gb300.adjoint import AreaMeanStreamfunction, ForcingGradient
+    c = gradient_case
+    fg = ForcingGradient(c.m, None, nsteps=36, precision="fp32")
+    fg.response = AreaMeanStreamfunction(fg.step.sp, c.m.vg)
+    J, g = fg.value_and_grad(c.heat)
+    assert g.dtype == torch_cuda.float32
+    assert fg.forward_steps == len(fg.calls)
+    assert abs(float(J) - c.J) <= 1e-5 * abs(c.J), (float(J), c.J)
+    assert float((g.double() - c.grad).abs().max()) <= 1e-4 * float(c.grad.abs().max())

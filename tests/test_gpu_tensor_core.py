@@ -1,7 +1,8 @@
-"""The Legendre analysis and synthesis on the tensor cores (tcgen05,
-bfloat16 split operands, FP32 accumulation in tensor memory) against FP64
-numpy restatements of the same contractions, next to the FP32 FMA kernels
-they replace; and whole runs in the bf16 modes against the FP64 path."""
+"""The Legendre analysis and synthesis and the longitude analysis on the
+tensor cores (tcgen05, bfloat16 split operands, FP32 accumulation in tensor
+memory) against FP64 numpy restatements of the same contractions, next to
+the FP32 FMA kernels they replace; and whole runs in the bf16 modes (their
+default placement of the contractions) against the FP64 path."""
 
 import ctypes as C
 
@@ -34,6 +35,10 @@ def _stepper(torch, case, precision):
     m, _, _ = make_ensemble_model(bs, E, Config(precision=precision, **configs.plain_damping(K)),
                                   device="gb300", nlon=nlon, nlat=nlat, nmax=nmax, sigm=sigm)
     stp = m.stepper()
+    # the kernel tests run every contraction on the tensor cores, whatever
+    # the precision's default placement
+    stp.tc_off = 0
+    stp._desc = stp._oargs = None
     stp.set_timesteps([1200.0])
     return stp
 
@@ -131,8 +136,6 @@ def test_longitude_analysis_kernel_vs_fp64(torch, case):
         stp = _stepper(torch, case, prec)
         if prec != "fp32":
             assert stp.tc_dft is not None
-            stp.tc_off = 0
-            stp._desc = stp._oargs = None
         if ref is None:
             jfac = stp.jfac.double().cpu().numpy()
             ref = _oracle_longitude_analysis(g9.astype(np.float64), jfac, M)

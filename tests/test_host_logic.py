@@ -254,12 +254,15 @@ def test_tensor_core_longitude_table_image_layout():
     """The tc_dft table image: per 16-longitude step three bfloat16 pieces of
     the 128 x 16 tile W[2m][i] = cos(2 pi m i / I) / I, W[2m+1][i] =
     -sin(2 pi m i / I) / I (zero past nmax), each element at the byte the
-    header gives, pieces summing to the FP64 value to 2^-24."""
+    header gives, pieces summing to the FP64 value to 2^-24; then the FP32
+    cos(2 pi t / I) table of the surface rows."""
     from lbm_isca_gb300.stepper import tc_dft_image
     for (I, N) in ((64, 21), (128, 42)):
         img = tc_dft_image(N, I).numpy().view(np.uint16)
         KS = I // 16
-        assert img.size == KS * 3 * 128 * 16
+        assert img.size == KS * 3 * 128 * 16 + 2 * I
+        cs = img[KS * 3 * 128 * 16:].copy().view(np.float32)
+        assert np.array_equal(cs, np.cos(2.0 * np.pi * np.arange(I) / I).astype(np.float32))
 
         def bf16(u):
             return (u.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
