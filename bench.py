@@ -88,10 +88,11 @@ def parse():
     ap.add_argument("--fd-dirs", type=int, default=16,
                     help="central-difference directions checked by --adjoint")
     ap.add_argument("--conditioning", action="store_true",
-                    help="conditioning of the 30-day problem: FP64 against FP64 with every "
-                         "heating rounded to FP32 (a relative input change below 2^-24), next "
-                         "to FP32 against FP64, T42L20 x 128 members (seed 2) and T85L40 x 8, "
-                         "reference dynamics and strictly linear, instead of the bench")
+                    help="conditioning of the 30-day problem: FP64 against FP64 with the "
+                         "heatings rounded to FP32, and with the day-10 state kicked by one "
+                         "FP32-sized relative change, next to FP32 and bf16x3 against FP64; "
+                         "the bench's 512-member T42L20 ensemble, T42L20 x 128 and T85L40 x 8 "
+                         "strictly linear; instead of the bench")
     ap.add_argument("--config4", action="store_true",
                     help="uneven batching: 48 T21L20 + 32 T42L20 + 16 T85L40 members (seed 4, "
                          "strictly linear), 20 days in one CUDA graph per stretch of steady "
@@ -427,33 +428,39 @@ def config4_measurement(torch, precision, days=20, groups=((64, 32, 21, 20, 48),
                        "members": g["stepper"].E, "choice": g["tile"]} for g in ge.groups]}
 
 
-def conditioning(torch, days=(10, 30)):
-    """How much of the FP32-against-FP64 difference the problem itself sets:
-    the same FP64 run with each heating rounded to FP32 (every input changed
-    by less than 2^-24 relatively, the size of one FP32 rounding) against
-    the unrounded FP64 run, beside the FP32 stepper against FP64; relative L2
-    per field over the packed spectral state of all members, at days 10 and
-    30.  Cases as the precision sweep: T42L20 x 128 members (dt 1200 s) with
-    the reference's dynamics (kinetic-energy term kept) and strictly linear,
-    T85L40 x 8 members (dt 600 s) strictly linear; seeded heatings (seed 2)."""
+def conditioning(torch, days=(10, 30), kick=1e-7):
+    """How much of the FP32-against-FP64 difference the problem itself sets.
+    Against the unperturbed FP64 run: (1) the FP64 run with each heating
+    rounded to FP32 (every input changed by less than 2^-24 relatively);
+    (2) the FP64 run whose state (both levels, spectral and grid ps') is
+    multiplied at the end of day 10 by (1 + ``kick`` n), n a seeded standard
+    normal per value -- one FP32-sized rounding of the developed state, then
+    exact FP64 arithmetic: its day-30 difference over ``kick`` is the growth
+    the problem gives to a single rounding error; beside the FP32 (FMA)
+    stepper and the bf16x3 stepper.  Relative L2 per field over all members,
+    and per member (worst field) the median, maximum and share within 1e-5.
+    Cases: the bench's own T42L20 ensemble (512 members, heatings seed 1, the
+    reference's dynamics with the kinetic-energy term), T42L20 x 128 members
+    strictly linear (seed 2), T85L40 x 8 members strictly linear (seed 2,
+    dt 600 s)."""
     from lbm_isca_gb300 import configs
     from lbm_isca_gb300.ensemble import make_ensemble_model
     from lbm_isca_gb300.model import Config
     out = {}
-    # (T85L40 with the reference dynamics grows without bound by day 14, in
-    # FP64 as in FP32: not a conditioning case)
-    cases = [(128, 64, 42, 20, 128, 1200.0, False), (128, 64, 42, 20, 128, 1200.0, True),
-             (256, 128, 85, 40, 8, 600.0, True)]
-    for (nlon, nlat, nmax, K, E, delt, lin) in cases:
+    cases = [("T42L20_bench_ensemble", 128, 64, 42, 20, 512, 1200.0, False, SEED),
+             ("T42L20_strictly_linear", 128, 64, 42, 20, 128, 1200.0, True, 2),
+             ("T85L40_strictly_linear", 256, 128, 85, 40, 8, 600.0, True, 2)]
+    for (label, nlon, nlat, nmax, K, E, delt, lin, seed) in cases:
         sigm = configs.equal_sigma_half_levels(K)
         bs = configs.solid_body_basic_state(nlon, nlat, sigm)
-        heats, _ = configs.ensemble_heating(nlon, nlat, sigm, E, seed=2)
+        heats, _ = configs.ensemble_heating(nlon, nlat, sigm, E, seed=seed)
         spd = int(round(86400.0 / delt))
         runs = {}
         for name, prec, h in (("fp64", "fp64", heats),
                               ("fp64_input_rounded", "fp64",
                                heats.astype(np.float32).astype(np.float64)),
-                              ("fp32", "fp32", heats)):
+                              ("fp64_kicked_day10", "fp64", heats),
+                              ("fp32", "fp32", heats), ("bf16x3", "bf16x3", heats)):
             cfg = Config(ndays=max(days), precision=prec,
                          **dict(configs.plain_damping(K), delt=delt, strictly_linear=lin))
             m, _, _ = make_ensemble_model(bs, E, cfg, device="cuda", nlon=nlon, nlat=nlat,
@@ -470,24 +477,41 @@ def conditioning(torch, days=(10, 30)):
                 stp.run(sched[done:upto], use_graph=True)
                 done = upto
                 torch.cuda.synchronize()
+                # copies: .to() of an FP64 state would return a view of it
                 snaps[d] = (None if not stp.check_finite() else
-                            {"vor": stp.sa3[:, 0].to(torch.complex128),
-                             "div": stp.sa3[:, 1].to(torch.complex128),
-                             "t": stp.sa3[:, 2].to(torch.complex128),
-                             "pi": stp.sas[:, 0].to(torch.complex128)})
+                            {k: x.to(torch.complex128, copy=True) for k, x in
+                             (("vor", stp.sa3[:, 0]), ("div", stp.sa3[:, 1]),
+                              ("t", stp.sa3[:, 2]), ("pi", stp.sas[:, 0]))})
+                if name == "fp64_kicked_day10" and d == 10:
+                    stp.flush()
+                    g = torch.Generator(device="cuda").manual_seed(7)
+                    for x in (stp.sa3, stp.sb3, stp.sas, stp.psa, stp.psb):
+                        n = torch.randn(x.shape, generator=g, device="cuda", dtype=torch.float64)
+                        x.mul_(1.0 + kick * n)
             runs[name] = snaps
             del m, stp
-        rec = {"members": E, "dt_s": delt, "strictly_linear": lin}
+        rec = {"members": E, "dt_s": delt, "strictly_linear": lin, "heating_seed": seed,
+               "kick": kick}
         for d in sorted(days):
             r = runs["fp64"][d]
-            for name in ("fp64_input_rounded", "fp32"):
+            for name in ("fp64_input_rounded", "fp64_kicked_day10", "fp32", "bf16x3"):
                 x = runs[name][d]
                 if r is None or x is None:
                     rec[f"{name}_day{d}"] = "non-finite"
                     continue
-                rec[f"{name}_day{d}"] = {k: float(torch.linalg.norm(x[k] - r[k]) /
-                                                  torch.linalg.norm(r[k])) for k in r}
-        out[f"T{nmax}L{K}" + ("_strictly_linear" if lin else "_default")] = rec
+                e, mem = {}, None
+                for k in r:
+                    e[k] = float(torch.linalg.norm(x[k] - r[k]) / torch.linalg.norm(r[k]))
+                    dims = tuple(range(1, r[k].dim()))
+                    pm = (torch.linalg.vector_norm(x[k] - r[k], dim=dims)
+                          / torch.linalg.vector_norm(r[k], dim=dims))
+                    mem = pm if mem is None else torch.maximum(mem, pm)
+                e["members_within_1e-5"] = float((mem <= 1e-5).double().mean())
+                e["member_median"] = float(mem.median())
+                e["member_max"] = float(mem.max())
+                e["worst_members"] = [int(i) for i in torch.argsort(mem, descending=True)[:5]]
+                rec[f"{name}_day{d}"] = e
+        out[label] = rec
     return out
 
 
@@ -907,9 +931,12 @@ def accuracy_block(args, torch, E, days=(10, 30)):
     and 30 days: one run of each precision through the fused stepper, the
     state taken at the end of day 10 (call 722) and of day 30 (call 2162);
     packed spectral coefficients of all members (vor, div, T: every level;
-    pi), q' as its absolute maximum (it stays 0: no moisture forcing)."""
+    pi), q' as its absolute maximum (it stays 0: no moisture forcing).  The
+    FP32 FMA path on the same members is reported beside it, and per member
+    (each member's relative L2, worst field) the share within 1e-5."""
     res = {}
-    for prec in ("fp64", args.precision):
+    precs = ["fp64", args.precision] + (["fp32"] if args.precision != "fp32" else [])
+    for prec in precs:
         m, heats = build_model(E, prec, torch, days=max(days))
         stp = m.stepper()
         sched = m._schedule(72 * max(days))
@@ -923,24 +950,32 @@ def accuracy_block(args, torch, E, days=(10, 30)):
             stp.run(sched[done:upto], use_graph=True)
             done = upto
             torch.cuda.synchronize()
-            snaps[d] = {"vor": stp.sa3[:, 0].to(torch.complex128),
-                        "div": stp.sa3[:, 1].to(torch.complex128),
-                        "t": stp.sa3[:, 2].to(torch.complex128),
-                        "pi": stp.sas[:, 0].to(torch.complex128),
-                        "q": stp.sa3[:, 3].to(torch.complex128)}
+            # copies: .to() of an FP64 state would return a view of it
+            snaps[d] = {k: x.to(torch.complex128, copy=True) for k, x in
+                        (("vor", stp.sa3[:, 0]), ("div", stp.sa3[:, 1]), ("t", stp.sa3[:, 2]),
+                         ("pi", stp.sas[:, 0]), ("q", stp.sa3[:, 3]))}
         if not stp.check_finite():
             raise FloatingPointError(f"accuracy run in {prec} produced non-finite values")
         res[prec] = snaps
         del m, stp
     out, worst = {}, {}
-    for d in sorted(days):
-        rel = {}
-        for k in ("vor", "div", "t", "pi"):
-            r, f = res["fp64"][d][k], res[args.precision][d][k]
-            rel[k] = float(torch.linalg.norm(f - r) / torch.linalg.norm(r))
-            worst[d] = max(worst.get(d, 0.0), rel[k])
-        rel["q_absmax"] = float(res[args.precision][d]["q"].abs().max())
-        out[f"accuracy_vs_fp64_day{d}"] = rel
+    for prec in precs[1:]:
+        tag = "" if prec == args.precision else f"_{prec}"
+        for d in sorted(days):
+            rel, mem = {}, None
+            for k in ("vor", "div", "t", "pi"):
+                r, f = res["fp64"][d][k], res[prec][d][k]
+                rel[k] = float(torch.linalg.norm(f - r) / torch.linalg.norm(r))
+                dims = tuple(range(1, r.dim()))
+                pm = torch.linalg.vector_norm(f - r, dim=dims) / torch.linalg.vector_norm(r, dim=dims)
+                mem = pm if mem is None else torch.maximum(mem, pm)
+                if prec == args.precision:
+                    worst[d] = max(worst.get(d, 0.0), rel[k])
+            rel["q_absmax"] = float(res[prec][d]["q"].abs().max())
+            rel["members_within_1e-5"] = float((mem <= 1e-5).double().mean())
+            rel["member_median"] = float(mem.median())
+            rel["member_max"] = float(mem.max())
+            out[f"accuracy{tag}_vs_fp64_day{d}"] = rel
     out["accuracy_max_rel_l2"] = {f"day{d}": v for d, v in worst.items()}
     out["accuracy_within_1e-5"] = {f"day{d}": bool(v <= 1e-5) for d, v in worst.items()}
     out["accuracy_members"] = E

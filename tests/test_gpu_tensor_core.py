@@ -249,3 +249,33 @@ def test_bf16_ensemble_against_fp64_at_day10(torch, precision, tol):
         e = float(torch.linalg.norm(f - r) / torch.linalg.norm(r))
         assert e <= tol, (k, e)
     assert float(out[precision]["q"].abs().max()) == 0.0
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "bf16split"])
+def test_members_independent_of_ensemble_size(torch, precision):
+    """Every contraction on the tensor cores: the first two members of a
+    32-member ensemble (13 units per persistent CTA, so the operand rings and
+    the two accumulator sets cycle many times) step bit for bit like a
+    2-member ensemble with the same heatings, over 24 steps."""
+    from lbm_isca_gb300 import Config
+    from lbm_isca_gb300.ensemble import make_ensemble_model
+    sigm = configs.equal_sigma_half_levels(20)
+    bs = configs.solid_body_basic_state(128, 64, sigm)
+    heats, _ = configs.ensemble_heating(128, 64, sigm, 32, seed=3)
+    got = {}
+    for E in (2, 32):
+        m, _, _ = make_ensemble_model(
+            bs, E, Config(ndays=1.0, precision=precision, tc_off=0, **configs.plain_damping(20)),
+            device="gb300", nlon=128, nlat=64, nmax=42, sigm=sigm)
+        stp = m.stepper()
+        sched = m._schedule(24)
+        stp.set_timesteps(sorted({dt for dt, _ in sched}))
+        stp.set_forcing(frc_t=m._spec_forcing(torch.as_tensor(heats[:E], device="cuda"), True),
+                        per_member=True)
+        stp.load_zero()
+        stp.run(sched, use_graph=True)
+        torch.cuda.synchronize()
+        assert stp.check_finite()
+        got[E] = (stp.sa3[:2].clone(), stp.sas[:2].clone(), stp.psa[:2].clone())
+    for a, b in zip(got[2], got[32]):
+        assert torch.equal(a, b)
