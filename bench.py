@@ -512,6 +512,7 @@ def conditioning(torch, days=(10, 30), kick=1e-7):
                 e["worst_members"] = [int(i) for i in torch.argsort(mem, descending=True)[:5]]
                 rec[f"{name}_day{d}"] = e
         out[label] = rec
+        print(json.dumps({"conditioning_case": {label: rec}}), flush=True)
     return out
 
 

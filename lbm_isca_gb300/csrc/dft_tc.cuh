@@ -31,7 +31,8 @@
 //
 // Roles of k_fdft_tc (one persistent CTA per SM): warp 0 loads the table
 // image once and prefetches units into L2; warp 1 TMEM and MMA issue; warps
-// 2..17 split the grid rows; warps 18..21 the epilogue.  Bounded waits as in
+// 2..13 split the grid rows; warps 14..21 the epilogue (each TMEM lane
+// quarter read by two warps, one per half of the levels).  Bounded waits as in
 // legendre_tc.cuh.  Supported: nlon <= 128 (the table's 2 (nmax + 1) <= 128
 // lanes), nlon a power of two, and 9 kmax <= 256 rows.
 #pragma once
@@ -41,8 +42,13 @@
 namespace lbm {
 
 constexpr int FTC_BSLOTS = 4;
-constexpr int FTC_CONV_WARPS = 16;
-constexpr int FTC_THREADS = 32 * (2 + FTC_CONV_WARPS + 4);
+constexpr int FTC_CONV_WARPS = 12;     // 384 threads, at most two items each (2 NR <= 512)
+constexpr int FTC_EPI_WARPS = 8;       // two warps per TMEM lane quarter, half the levels each
+constexpr int FTC_CONV = 32 * FTC_CONV_WARPS;
+constexpr int FTC_EPI = 32 * FTC_EPI_WARPS;
+constexpr int FTC_THREADS = 32 * (2 + FTC_CONV_WARPS + FTC_EPI_WARPS);
+static_assert(FTC_EPI == 256, "the epilogue's named barrier counts 256 threads");
+static_assert(2 * FTC_CONV >= 512, "two items per conversion thread cover 2 NR <= 512");
 constexpr int FTC_PREFETCH = 2;        // units of grid rows pulled into L2 ahead
 
 // Floats per wavenumber in the epilogue's staging area: the K x 7 complex of
@@ -109,7 +115,7 @@ __global__ void __launch_bounds__(FTC_THREADS, 1)
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(smem_addr(&sm->accfull[i]), 1);
-      mbar_init(smem_addr(&sm->accempty[i]), 4);
+      mbar_init(smem_addr(&sm->accempty[i]), FTC_EPI_WARPS);
     }
     mbar_init(smem_addr(&sm->done), 1);
     fence_mbar_init();
@@ -176,31 +182,39 @@ __global__ void __launch_bounds__(FTC_THREADS, 1)
     }
   } else if (warp < 2 + FTC_CONV_WARPS) {
     // ---------------- conversion: grid rows -> B tiles ----------------
-    // One (B row, 8-longitude chunk) item per thread (2 NR <= 512 items):
-    // the 8 lanes of a quarter warp take 8 consecutive B rows of one chunk,
-    // so each 16-byte store of a quarter warp fills one 128-byte core-matrix
-    // row group (no bank conflicts).  The next step's rows are loaded into
-    // registers before this step's are split (the loads' latency is hidden
-    // behind the split and the wait for a free slot).
+    // (B row, 8-longitude chunk) items it = ct and ct + FTC_CONV per thread
+    // (2 NR <= 512 items): the 8 lanes of a quarter warp take 8 consecutive B
+    // rows of one chunk, so each 16-byte store of a quarter warp fills one
+    // 128-byte core-matrix row group (no bank conflicts).  The next step's
+    // rows are loaded into registers before this step's are split (the
+    // loads' latency is hidden behind the split and the wait for a slot).
     const int ct = threadIdx.x - 64;
-    const int chk = (ct >> 3) & 1;
-    const int br = (ct & 7) | ((ct >> 4) << 3);  // B row (field f = br / K, level br % K)
-    const bool live = br < NR;                   // padding rows past R stay zero
-    const bool data = br < R;
-    const int q = 9 * (br % K) + br / K;         // its level row: ftc_brow(q, K) == br
-    const unsigned off = tile_offset(br, chk * 8);
-    auto load = [&](int u, int s, float4& x0, float4& x1) {
-      if (data && u < pl.nunits) {
+    int br[2], chk[2], q[2];
+    bool live[2], data[2];
+    unsigned off[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int it = ct + h * FTC_CONV;
+      chk[h] = (it >> 3) & 1;
+      br[h] = (it & 7) | ((it >> 4) << 3);       // B row (field f = br / K, level br % K)
+      live[h] = it < 2 * NR;                     // padding rows past R stay zero
+      data[h] = live[h] && br[h] < R;
+      q[h] = 9 * (br[h] % K) + br[h] / K;        // its level row: ftc_brow(q, K) == br
+      off[h] = tile_offset(br[h], chk[h] * 8);
+    }
+    auto load = [&](int h, int u, int s, float4& x0, float4& x1) {
+      if (data[h] && u < pl.nunits) {
         const float4* src = reinterpret_cast<const float4*>(
-            g9 + (size_t)u * unit_floats + (size_t)(2 + q) * I + s * 16 + chk * 8);
+            g9 + (size_t)u * unit_floats + (size_t)(2 + q[h]) * I + s * 16 + chk[h] * 8);
         x0 = __ldg(src);
         x1 = __ldg(src + 1);
       } else {
         x0 = x1 = make_float4(0.f, 0.f, 0.f, 0.f);
       }
     };
-    float4 n0, n1;
-    load(blockIdx.x, 0, n0, n1);
+    float4 n0[2], n1[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) load(h, blockIdx.x, 0, n0[h], n1[h]);
     unsigned a = 0;
     for (int u = blockIdx.x; u < pl.nunits && ok; u += gridDim.x) {
       if (ct == 0) {
@@ -210,13 +224,21 @@ __global__ void __launch_bounds__(FTC_THREADS, 1)
       }
       for (int s = 0; s < KS && ok; ++s, ++a) {
         const int slot = a % FTC_BSLOTS;
-        const float x[8] = {n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, n1.z, n1.w};
-        if (s + 1 < KS) load(u, s + 1, n0, n1);
-        else load(u + gridDim.x, 0, n0, n1);
+        float x[2][8];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          x[h][0] = n0[h].x; x[h][1] = n0[h].y; x[h][2] = n0[h].z; x[h][3] = n0[h].w;
+          x[h][4] = n1[h].x; x[h][5] = n1[h].y; x[h][6] = n1[h].z; x[h][7] = n1[h].w;
+          if (s + 1 < KS) load(h, u, s + 1, n0[h], n1[h]);
+          else load(h, u + gridDim.x, 0, n0[h], n1[h]);
+        }
         ok = warp_wait(smem_addr(&sm->bempty[slot]), ((a / FTC_BSLOTS) & 1u) ^ 1u, err, ATC_ERR);
         if (!ok) break;
         unsigned char* bt = bring + slot * bslot;
-        if (live) split3_store8(x, bt + off, bt + NR * 32 + off, bt + 2 * NR * 32 + off);
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+          if (live[h])
+            split3_store8(x[h], bt + off[h], bt + NR * 32 + off[h], bt + 2 * NR * 32 + off[h]);
         fence_async_smem();
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_addr(&sm->bfull[slot]));
@@ -224,10 +246,12 @@ __global__ void __launch_bounds__(FTC_THREADS, 1)
     }
   } else {
     // ---------------- epilogue ----------------
-    const int q4 = warp & 3;
+    const int q4 = warp & 3;                                    // TMEM lane quarter
     const int L = 32 * q4 + lane, m = L >> 1, c = L & 1;
     const bool live = m < M;
-    const int et = threadIdx.x - 32 * (2 + FTC_CONV_WARPS);     // 0..127
+    const int et = threadIdx.x - 32 * (2 + FTC_CONV_WARPS);     // 0..FTC_EPI-1
+    const int KH = (K + 1) / 2, klo = (et >= 128) ? KH : 0;     // this warp's levels
+    const int khi = (et >= 128) ? K : KH;
     const int SS = ftc_stage_stride(K);
     unsigned ul = 0;
     for (int u = blockIdx.x; u < pl.nunits && ok; u += gridDim.x, ++ul) {
@@ -245,7 +269,7 @@ __global__ void __launch_bounds__(FTC_THREADS, 1)
       asm volatile(
           "{\n\t.reg .pred pb, po;\n\t"
           "setp.eq.u32 pb, %1, 0;\n\t"
-          "bar.red.or.pred po, 1, 128, pb;\n\t"
+          "bar.red.or.pred po, 1, 256, pb;\n\t"
           "selp.u32 %0, 1, 0, po;\n\t}\n"
           : "=r"(bad)
           : "r"(ok ? 1u : 0u)
@@ -256,7 +280,7 @@ __global__ void __launch_bounds__(FTC_THREADS, 1)
       }
       tc_fence_after();
       const unsigned tl = tbase + ((unsigned)(32 * q4) << 16) + (unsigned)(b * NR);
-      for (int k = 0; k < K; ++k) {
+      for (int k = klo; k < khi; ++k) {
         unsigned r[9];
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%9];\n"
@@ -299,13 +323,13 @@ __global__ void __launch_bounds__(FTC_THREADS, 1)
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(smem_addr(&sm->accempty[b]));
-      asm volatile("bar.sync 1, 128;\n" ::: "memory");
+      asm volatile("bar.sync 1, 256;\n" ::: "memory");
       // staged rows -> af: for each m, K * 7 complex contiguous
       const int rowf = K * AF_N * 2;                       // floats per m
       const int q4 = rowf / 4;                             // float4 per m
       const int n4 = M * q4;
       float* afe = reinterpret_cast<float*>(d.af) + (((size_t)e * M) * J + j) * rowf;
-      for (int x = et; x < n4; x += 128) {
+      for (int x = et; x < n4; x += FTC_EPI) {
         const int mm = x / q4, w = x - mm * q4;
         *reinterpret_cast<float4*>(afe + (size_t)mm * J * rowf + 4 * w) =
             *reinterpret_cast<const float4*>(stage + (size_t)mm * SS + 4 * w);
