@@ -49,7 +49,7 @@ constexpr int FTC_EPI = 32 * FTC_EPI_WARPS;
 constexpr int FTC_THREADS = 32 * (2 + FTC_CONV_WARPS + FTC_EPI_WARPS);
 static_assert(FTC_EPI == 256, "the epilogue's named barrier counts 256 threads");
 static_assert(2 * FTC_CONV >= 512, "two items per conversion thread cover 2 NR <= 512");
-constexpr int FTC_PREFETCH = 2;        // units of grid rows pulled into L2 ahead
+constexpr int FTC_PREFETCH = 1;        // units of grid rows pulled into L2 ahead (swept: 0-6)
 
 // Floats per wavenumber in the epilogue's staging area: the K x 7 complex of
 // a unit's af row plus 4, so that the 16 wavenumbers of a warp's stores fall
