@@ -818,8 +818,10 @@ def main():
         e2e = end_to_end(args, E, heats, torch)
 
     # ---- extras: accuracy vs FP64 and the plain single-member FP64 rate ----
+    # (N = 1 only, like the CPU baseline: the FP64 reference over all members
+    # and 30 days takes minutes, which other ranks must not wait through)
     extras = {}
-    if rank == 0 and not args.no_extras:
+    if rank == 0 and world == 1 and not args.no_extras:
         extras = side_measurements(args, torch)
 
     if rank == 0:
@@ -938,6 +940,7 @@ def accuracy_block(args, torch, E, days=(10, 30)):
     res = {}
     precs = ["fp64", args.precision] + (["fp32"] if args.precision != "fp32" else [])
     for prec in precs:
+        t0 = time.perf_counter()
         m, heats = build_model(E, prec, torch, days=max(days))
         stp = m.stepper()
         sched = m._schedule(72 * max(days))
@@ -959,6 +962,8 @@ def accuracy_block(args, torch, E, days=(10, 30)):
             raise FloatingPointError(f"accuracy run in {prec} produced non-finite values")
         res[prec] = snaps
         del m, stp
+        print(f"accuracy run {prec}: {time.perf_counter() - t0:.1f} s", file=sys.stderr,
+              flush=True)
     out, worst = {}, {}
     for prec in precs[1:]:
         tag = "" if prec == args.precision else f"_{prec}"

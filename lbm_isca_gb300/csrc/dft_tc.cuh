@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(FTC_THREADS, 1)
       const float wdm = wd * float(m);
       const int b = ul & 1;
       ok = warp_wait(smem_addr(&sm->accfull[b]), (ul >> 1) & 1u, err, ATC_ERR);
-      // one decision for the four epilogue warps (a named-barrier OR), which
+      // one decision for the eight epilogue warps (a named-barrier OR), which
       // also orders this unit's staging writes after every thread's copy-out
       // of the previous unit
       unsigned bad;
@@ -326,11 +326,11 @@ __global__ void __launch_bounds__(FTC_THREADS, 1)
       asm volatile("bar.sync 1, 256;\n" ::: "memory");
       // staged rows -> af: for each m, K * 7 complex contiguous
       const int rowf = K * AF_N * 2;                       // floats per m
-      const int q4 = rowf / 4;                             // float4 per m
-      const int n4 = M * q4;
+      const int nq = rowf / 4;                             // float4 per m
+      const int n4 = M * nq;
       float* afe = reinterpret_cast<float*>(d.af) + (((size_t)e * M) * J + j) * rowf;
       for (int x = et; x < n4; x += FTC_EPI) {
-        const int mm = x / q4, w = x - mm * q4;
+        const int mm = x / nq, w = x - mm * nq;
         *reinterpret_cast<float4*>(afe + (size_t)mm * J * rowf + 4 * w) =
             *reinterpret_cast<const float4*>(stage + (size_t)mm * SS + 4 * w);
       }
