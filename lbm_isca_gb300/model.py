@@ -83,8 +83,9 @@ class Config:
     # --- GB300 path ----------------------------------------------------------
     precision: str = "fp64"       # "fp64" | "fp32" | "bf16x3" | "bf16split": working
                                   # precision of the step; the bf16 modes keep the FP32
-                                  # state and run the Legendre analysis on the tensor
-                                  # cores (3-way bf16 split, 6 or 3 products)
+                                  # state and run contractions on the tensor cores
+                                  # (bf16 split, 6 or 3 products): bf16x3 the
+                                  # longitude analysis, bf16split all three
     tc_off: int = -1              # bf16 modes: contractions kept on the FMA pipes (bit 0
                                   # Legendre analysis, 1 synthesis, 2 longitude
                                   # analysis); -1: the precision's default

@@ -147,8 +147,8 @@ class EnsembleStepper:
         self.cd = torch.complex128 if precision == "fp64" else torch.complex64
         self.prec_id = _lib.LBM_F64 if precision == "fp64" else _lib.LBM_F32
         self.legendre = self.LEGENDRE[precision]
-        # tile choices of the tensor-core kernels (see tune()): which of the
-        # analysis / synthesis stay on the FMA kernels, members per MMA tile
+        # placement and tiles of the tensor-core kernels (autotune.tune()):
+        # which contractions stay on the FMA kernels, members per MMA tile
         self.tc_off = int(self.TC_OFF.get(precision, 0) if tc_off is None else tc_off)
         self.tc_g = 0
         if not 0 <= self.tc_off <= 7:
