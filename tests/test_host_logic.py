@@ -275,3 +275,36 @@ def test_tensor_core_longitude_table_image_layout():
                     off = (L // 8) * 128 + (kk // 8) * 64 + (L % 8) * 8 + kk % 8
                     val = sum(bf16(img[(s * 3 + p) * 2048 + off]) for p in range(3))
                     assert abs(val - ref) <= 2.0 ** -24 * abs(ref) + 1e-36, (I, s, L, kk)
+
+
+def test_autotune_candidates_keep_the_precision_placement():
+    """bf16x3 never clears the Legendre bits (their tensor-core accumulation
+    breaks its 1e-5 gate); bf16split may place every contraction; the
+    longitude-analysis bit is free only where its tensor-core table exists."""
+    import types
+    from lbm_isca_gb300.autotune import candidates
+    mk = lambda prec, dft: types.SimpleNamespace(K=20, E=32, precision=prec,   # noqa: E731
+                                                 tc_dft=object() if dft else None)
+    c3 = candidates(mk("bf16x3", True))
+    assert c3 and all(off & 3 == 3 for off, _ in c3)
+    assert {off for off, _ in c3} == {3, 7}
+    cs = candidates(mk("bf16split", True))
+    assert {off for off, _ in cs} == set(range(8))
+    assert {g for _, g in cs} == {0, 3, 1}
+    assert all(off & 4 for off, _ in candidates(mk("bf16split", False)))
+
+
+def test_launches_per_step():
+    """FP64: four kernels; FP32: six; each contraction on the tensor cores
+    adds the launch of its surface fields' FMA kernel."""
+    import types
+    from lbm_isca_gb300.stepper import EnsembleStepper
+    f = EnsembleStepper.launches_per_step
+    ns = lambda prec, leg, off, dft: types.SimpleNamespace(   # noqa: E731
+        precision=prec, legendre=leg, tc_off=off, tc_dft=object() if dft else None)
+    assert f(ns("fp64", 0, 0, False)) == 4
+    assert f(ns("fp32", 0, 0, False)) == 6
+    assert f(ns("bf16x3", 6, 3, True)) == 7
+    assert f(ns("bf16x3", 6, 0, True)) == 9
+    assert f(ns("bf16split", 3, 0, False)) == 8
+    assert f(ns("bf16x3", 6, 7, True)) == 6
