@@ -93,6 +93,9 @@ def parse():
                          "FP32-sized relative change, next to FP32 and bf16x3 against FP64; "
                          "the bench's 512-member T42L20 ensemble, T42L20 x 128 and T85L40 x 8 "
                          "strictly linear; instead of the bench")
+    ap.add_argument("--config4-adjoint", action="store_true",
+                    help="--config4: then each group's gradient of the config-3 response "
+                         "(precision from --adjoint-precision)")
     ap.add_argument("--config4", action="store_true",
                     help="uneven batching: 48 T21L20 + 32 T42L20 + 16 T85L40 members (seed 4, "
                          "strictly linear), 20 days in one CUDA graph per stretch of steady "
@@ -390,7 +393,8 @@ def precision_sweep(torch):
 
 def config4_measurement(torch, precision, days=20, groups=((64, 32, 21, 20, 48),
                                                              (128, 64, 42, 20, 32),
-                                                             (256, 128, 85, 40, 16))):
+                                                             (256, 128, 85, 40, 16)),
+                        adjoint=None):
     """Members of three truncations stepped together (GroupedEnsemble): the
     seeded heatings of every group drawn in order from one generator (seed
     4), solid-body basic states, plain damping, strictly linear dynamics (the
@@ -420,12 +424,62 @@ def config4_measurement(torch, precision, days=20, groups=((64, 32, 21, 20, 48),
     ms = e0.elapsed_time(e1)
     finite = ge.check_finite()
     E = ge.members
-    return {"workload": "48 T21L20 + 32 T42L20 + 16 T85L40 members, seeded heatings (seed 4), "
-                        f"strictly linear, dt 1200 s, {days} days, {precision}",
-            "members": E, "steps": nsteps, "seconds": ms / 1000.0,
-            "member_steps_per_s": E * nsteps / (ms / 1000.0), "finite": finite,
-            "tiles": [{"grid": f"T{g['stepper'].N}L{g['stepper'].K}",
-                       "members": g["stepper"].E, "choice": g["tile"]} for g in ge.groups]}
+    out = {"workload": "48 T21L20 + 32 T42L20 + 16 T85L40 members, seeded heatings (seed 4), "
+                       f"strictly linear, dt 1200 s, {days} days, {precision}",
+           "members": E, "steps": nsteps, "seconds": ms / 1000.0,
+           "member_steps_per_s": E * nsteps / (ms / 1000.0), "finite": finite,
+           "tiles": [{"grid": f"T{g['stepper'].N}L{g['stepper'].K}",
+                      "members": g["stepper"].E, "choice": g["tile"]} for g in ge.groups]}
+    if adjoint:
+        out["adjoint"] = config4_adjoint(torch, ge, nsteps, adjoint)
+    return out
+
+
+def config4_adjoint(torch, ge, nsteps, precision):
+    """The adjoint half of config 4: for each truncation group, every
+    member's gradient of its own config-3 response (area-mean psi' at sigma
+    0.25 over 30-60N 150-210E at the end of the run) with respect to its
+    heating, over the same calls as the forward run, by the checkpointed
+    adjoint in `precision` (every state stored where the group's trajectory
+    fits in half the free HBM, else as many as fit on the binomial schedule);
+    each group reversed as one batched model, one group after another (not
+    inside the grouped graph).  Seconds of one gradient against one forward
+    run of the same calls, member-gradients per second."""
+    from lbm_isca_gb300.adjoint import AreaMeanStreamfunction, ForcingGradient
+    res = []
+    for g in ge.groups:
+        m = g["model"]
+        h = torch.as_tensor(g["heats"], device="cuda")
+
+        def make(n, **kw):
+            fg = ForcingGradient(m, None, nsteps=n, precision=precision, **kw)
+            fg.response = AreaMeanStreamfunction(fg.step.sp, m.vg)
+            return fg
+
+        warm = make(4, snaps=2)
+        warm.value_and_grad(h)                       # captures every graph variant
+        fg = make(nsteps)
+        fg._fg, fg._ag = warm._fg, warm._ag
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Jf = fg.value(h)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        J, grad = fg.value_and_grad(h)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        E = int(h.shape[0])
+        res.append({"grid": f"T{m.sp.nmax}L{m.vg.kmax}", "members": E,
+                    "calls": len(fg.calls), "stored_states": fg.snaps,
+                    "forward_steps_in_gradient": fg.forward_steps,
+                    "forward_s": t1 - t0, "gradient_s": t2 - t1,
+                    "gradient_over_forward": (t2 - t1) / (t1 - t0),
+                    "member_gradients_per_s": E / (t2 - t1),
+                    "J_forward_equals_gradient_sweep": bool(torch.equal(Jf, J)),
+                    "finite": bool(torch.isfinite(grad).all())})
+        del warm, fg, grad
+        torch.cuda.empty_cache()
+    return res
 
 
 def conditioning(torch, days=(10, 30), kick=1e-7):
@@ -629,10 +683,10 @@ def adjoint_measurement(torch, days=20.0, snaps=None, fd_dirs=16, nsteps=None,
     }
 
 
-def adjoint_batched_measurement(torch, nmem, nsteps, snaps=None):
+def adjoint_batched_measurement(torch, nmem, nsteps, snaps=None, precision="fp64"):
     """One gradient of ``nmem`` members (seeded ensemble heatings, T42L20,
-    FP64, each member its own response) reversed together, against one
-    single-member gradient over the same calls."""
+    each member its own response) reversed together, against one
+    single-member gradient over the same calls, in `precision`."""
     from lbm_isca_gb300 import LBM, Config, Spectral, VerticalGrid, configs
     from lbm_isca_gb300.adjoint import AreaMeanStreamfunction, ForcingGradient
     from lbm_isca_gb300.ensemble import make_ensemble_model
@@ -652,10 +706,13 @@ def adjoint_batched_measurement(torch, nmem, nsteps, snaps=None):
         else:
             m, sp, vg = make_ensemble_model(bs, E, cfg(), device="cuda", sigm=sigm)
             h = heats
-        resp = AreaMeanStreamfunction(sp, vg)
-        warm = ForcingGradient(m, resp, nsteps=4, snaps=2)
+        def make(n, **kw):
+            g = ForcingGradient(m, None, nsteps=n, precision=precision, **kw)
+            g.response = AreaMeanStreamfunction(g.step.sp, vg)
+            return g
+        warm = make(4, snaps=2)
         warm.value_and_grad(h)
-        fg = ForcingGradient(m, resp, nsteps=nsteps, snaps=snaps)
+        fg = make(nsteps, snaps=snaps)
         fg._fg, fg._ag = warm._fg, warm._ag
         out[f"{name}_snaps"] = fg.snaps
         torch.cuda.synchronize()
@@ -683,7 +740,8 @@ def main():
         import torch
         torch.cuda.set_device(0)
         out = adjoint_batched_measurement(torch, args.adjoint_members,
-                                          args.adjoint_steps or 72)
+                                          args.adjoint_steps or 72,
+                                          precision=args.adjoint_precision)
         print(json.dumps({"adjoint_batched": out}), flush=True)
         return
     if args.adjoint:
@@ -696,7 +754,9 @@ def main():
     if args.config4:
         import torch
         torch.cuda.set_device(0)
-        print(json.dumps({"config4": config4_measurement(torch, args.precision)}), flush=True)
+        print(json.dumps({"config4": config4_measurement(
+            torch, args.precision, adjoint=args.adjoint_precision if args.config4_adjoint
+            else None)}), flush=True)
         return
     if args.conditioning:
         import torch

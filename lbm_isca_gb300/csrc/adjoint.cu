@@ -51,11 +51,25 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_tendency_grid_adj(lbm_tend_adj_
   c.u0 = a.u0 ? P(a.u0) + p3 : nullptr;
   c.v0 = a.v0 ? P(a.v0) + p3 : nullptr;
   R work[5 * (KM + 1)];
+  // the adjoints are accumulated level by level (K x K scatters of the
+  // hydrostatic and tmtx transposes, the vertical-advection transposes):
+  // into thread-local arrays, whose elements the hardware interleaves across
+  // the threads of a warp, and written to the level-strided outputs once
+  R lu[KM], lv[KM], lt[KM], lq[KM], lvor[KM], ldiv[KM];
   lbm_adj::tendency_column_adjoint<R>(
       c, P(a.a_fu) + p3, P(a.a_fv) + p3, P(a.a_ke) + p3, P(a.a_gt) + p3, P(a.a_xu) + p3,
       P(a.a_xv) + p3, P(a.a_g) + p3, P(a.a_yu) + p3, P(a.a_yv) + p3, P(a.a_gt_pi)[col],
-      (R*)a.a_u + p3, (R*)a.a_v + p3, (R*)a.a_t + p3, (R*)a.a_q + p3, (R*)a.a_vor + p3,
-      (R*)a.a_div + p3, (R*)a.a_pix + col, (R*)a.a_piy + col, work);
+      lu, lv, lt, lq, lvor, ldiv, (R*)a.a_pix + col, (R*)a.a_piy + col, work);
+  R *ou = (R*)a.a_u + p3, *ov = (R*)a.a_v + p3, *ot = (R*)a.a_t + p3, *oq = (R*)a.a_q + p3,
+    *ovor = (R*)a.a_vor + p3, *odiv = (R*)a.a_div + p3;
+  for (int k = 0; k < K; ++k) {
+    ou[k] = lu[k];
+    ov[k] = lv[k];
+    ot[k] = lt[k];
+    oq[k] = lq[k];
+    ovor[k] = lvor[k];
+    odiv[k] = ldiv[k];
+  }
 }
 
 // One thread per (member, m, n, real/imaginary part).
