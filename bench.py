@@ -93,10 +93,11 @@ def parse():
                          "FP32-sized relative change, next to FP32 and bf16x3 against FP64; "
                          "the bench's 512-member T42L20 ensemble, T42L20 x 128 and T85L40 x 8 "
                          "strictly linear; instead of the bench")
-    ap.add_argument("--config4-adjoint", action="store_true",
-                    help="--config4: then each group's gradient of the config-3 response "
-                         "(precision from --adjoint-precision)")
-    ap.add_argument("--config4", action="store_true",
+    ap.add_argument("--uneven-groups-adjoint", action="store_true",
+                    help="--uneven-groups: then each group's gradient of the area-mean "
+                         "streamfunction response (sigma 0.25, 30-60N 150-210E; precision "
+                         "from --adjoint-precision)")
+    ap.add_argument("--uneven-groups", action="store_true",
                     help="uneven batching: 48 T21L20 + 32 T42L20 + 16 T85L40 members (seed 4, "
                          "strictly linear), 20 days in one CUDA graph per stretch of steady "
                          "steps, autotuned tensor-core tiles per truncation, instead of the "
@@ -391,7 +392,7 @@ def precision_sweep(torch):
     return out
 
 
-def config4_measurement(torch, precision, days=20, groups=((64, 32, 21, 20, 48),
+def uneven_groups_measurement(torch, precision, days=20, groups=((64, 32, 21, 20, 48),
                                                              (128, 64, 42, 20, 32),
                                                              (256, 128, 85, 40, 16)),
                         adjoint=None):
@@ -431,14 +432,14 @@ def config4_measurement(torch, precision, days=20, groups=((64, 32, 21, 20, 48),
            "tiles": [{"grid": f"T{g['stepper'].N}L{g['stepper'].K}",
                       "members": g["stepper"].E, "choice": g["tile"]} for g in ge.groups]}
     if adjoint:
-        out["adjoint"] = config4_adjoint(torch, ge, nsteps, adjoint)
+        out["adjoint"] = uneven_groups_adjoint(torch, ge, nsteps, adjoint)
     return out
 
 
-def config4_adjoint(torch, ge, nsteps, precision):
-    """The adjoint half of config 4: for each truncation group, every
-    member's gradient of its own config-3 response (area-mean psi' at sigma
-    0.25 over 30-60N 150-210E at the end of the run) with respect to its
+def uneven_groups_adjoint(torch, ge, nsteps, precision):
+    """The adjoint half of the uneven-truncation workload: for each group,
+    every member's gradient of its own response (area-mean psi' at sigma 0.25
+    over 30-60N 150-210E at the end of the run) with respect to its
     heating, over the same calls as the forward run, by the checkpointed
     adjoint in `precision` (every state stored where the group's trajectory
     fits in half the free HBM, else as many as fit on the binomial schedule);
@@ -751,11 +752,11 @@ def main():
                                   precision=args.adjoint_precision)
         print(json.dumps({"adjoint": out}), flush=True)
         return
-    if args.config4:
+    if args.uneven_groups:
         import torch
         torch.cuda.set_device(0)
-        print(json.dumps({"config4": config4_measurement(
-            torch, args.precision, adjoint=args.adjoint_precision if args.config4_adjoint
+        print(json.dumps({"uneven_groups": uneven_groups_measurement(
+            torch, args.precision, adjoint=args.adjoint_precision if args.uneven_groups_adjoint
             else None)}), flush=True)
         return
     if args.conditioning:

@@ -4,7 +4,7 @@ produced by running the reference package itself.
 
 Usage (where the reference checkout is available):
 
-    python tests/golden/make_golden_config0.py <path of the reference checkout>
+    python tests/golden/make_golden_t42l20_run.py <path of the reference checkout>
 
 The workload: T42 (128 x 64 Gaussian grid), 20 equally spaced sigma levels,
 the solid-body basic state of ``lbm_isca_gb300.configs`` (u = 15 cos(lat),
@@ -81,8 +81,8 @@ def main(refdir):
     model.run(mjo_forcing=Heating(), verbose=False)
     record("day30")
     out["calls"] = np.array(Heating.calls)
-    np.savez_compressed(os.path.join(HERE, "config0_t42l20.npz"), **out)
-    print(f"config0_t42l20.npz written ({Heating.calls} calls, {time.time() - t0:.0f} s)")
+    np.savez_compressed(os.path.join(HERE, "t42l20_reference_run.npz"), **out)
+    print(f"t42l20_reference_run.npz written ({Heating.calls} calls, {time.time() - t0:.0f} s)")
 
 
 if __name__ == "__main__":

@@ -3,8 +3,8 @@ own trajectory: the FP64 path to 1e-10 and the FP32 path to 1e-5 relative L2
 per prognostic field, after 10 and 30 model days (722 and 2162 calls of the
 step, model.py:213-247).
 
-Golden: tests/golden/config0_t42l20.npz, written by
-tests/golden/make_golden_config0.py from the reference package (solid-body
+Golden: tests/golden/t42l20_reference_run.npz, written by
+tests/golden/make_golden_t42l20_run.py from the reference package (solid-body
 basic state, elliptic heating at 0N 120E, plain damping, dt 1200 s, the
 reference's default dynamics)."""
 
@@ -52,8 +52,8 @@ def _packed(x, M=43):
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32", "bf16x3", "bf16split"])
 @pytest.mark.parametrize("day", [10, 30])
-def test_config0_t42l20_matches_reference_trajectory(torch, precision, day):
-    g = golden("config0_t42l20.npz")
+def test_t42l20_run_matches_reference_trajectory(torch, precision, day):
+    g = golden("t42l20_reference_run.npz")
     m, a = _run(precision, float(day))
     tol = TOL[precision]
     errs = {}
