@@ -87,6 +87,10 @@ def parse():
                          "against one single-member gradient instead")
     ap.add_argument("--fd-dirs", type=int, default=16,
                     help="central-difference directions checked by --adjoint")
+    ap.add_argument("--cpu-plans", action="store_true",
+                    help="CPU baselines on the host: one member with all BLAS threads "
+                         "(T42L20, T85L40) and the oracle batched over 512 members, "
+                         "instead of the bench")
     ap.add_argument("--conditioning", action="store_true",
                     help="conditioning of the 30-day problem: FP64 against FP64 with the "
                          "heatings rounded to FP32, and with the day-10 state kicked by one "
@@ -161,6 +165,60 @@ def host_cores():
         return len(os.sched_getaffinity(0))
     except Exception:
         return os.cpu_count() or 1
+
+
+def mem_available_bytes():
+    """MemAvailable of the host (Linux), or None."""
+    try:
+        with open("/proc/meminfo") as fh:
+            for line in fh:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return None
+
+
+def cpu_plans(budget_s=30.0, bytes_per_member=50e6):
+    """The CPU baselines besides the one-member-per-core throughput: (i) one
+    member with the BLAS threads on all host cores (numpy's default in this
+    process) at T42L20 and T85L40; (iii) the oracle batched over up to 512
+    members (its member axis, as make_ensemble_model(device="cpu") batches)
+    at T42L20, as many as fit in 30% of the host's available memory at
+    about `bytes_per_member` each (45 MB measured peak); each after one
+    warm-up step, timed over as many steps as fit in `budget_s` (at least
+    one)."""
+    from oracle import lbm_oracle as orc
+    from lbm_isca_gb300 import configs
+    avail = mem_available_bytes()
+    e_big = 512 if avail is None else max(1, min(512, int(0.3 * avail / bytes_per_member)))
+    out = {"cores": host_cores(), "mem_available_gb": None if avail is None else avail / 1e9}
+
+    def timed_steps(m, frc):
+        m.step(frc_t=frc)
+        t0 = time.perf_counter()
+        n = 0
+        while n == 0 or (time.perf_counter() - t0) < budget_s:
+            m.step(frc_t=frc)
+            n += 1
+        return n, time.perf_counter() - t0
+
+    for label, (nlon, nlat, nmax, K, E) in (("single_T42L20", (128, 64, 42, 20, None)),
+                                            ("single_T85L40", (256, 128, 85, 40, None)),
+                                            ("batched_T42L20", (128, 64, 42, 20, e_big))):
+        sigm = configs.equal_sigma_half_levels(K)
+        tr = orc.SphericalTransform(nlon, nlat, nmax)
+        lv = orc.SigmaLevels(sigm)
+        bs = configs.solid_body_basic_state(nlon, nlat, sigm)
+        heats, _ = configs.ensemble_heating(nlon, nlat, sigm, E or 1, seed=SEED)
+        m = orc.OracleModel(tr, lv, bs, orc.RunConfig(**configs.plain_damping(K)), nmem=E)
+        n, sec = timed_steps(m, heats if E else heats[0])
+        out[label] = {"members": E or 1, "steps": n, "seconds": sec,
+                      "ms_per_step": 1000.0 * sec / n,
+                      "member_steps_per_s": (E or 1) * n / sec}
+        print(json.dumps({"cpu_plan": {label: out[label]}}), file=sys.stderr, flush=True)
+        del m
+    return out
 
 
 def reference_arm(args):
@@ -758,6 +816,9 @@ def main():
         print(json.dumps({"uneven_groups": uneven_groups_measurement(
             torch, args.precision, adjoint=args.adjoint_precision if args.uneven_groups_adjoint
             else None)}), flush=True)
+        return
+    if args.cpu_plans:
+        print(json.dumps({"cpu_plans": cpu_plans()}), flush=True)
         return
     if args.conditioning:
         import torch
